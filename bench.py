@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Throughput of the 2-D electrostatic PIC step on GB300 (particle-steps/s).
+
+Workload (one "step" = one PIC time step: gather + push + fixed-point deposit
+of every particle, int64->float density, cuFFT R2C, k-space kernel, 2x C2R,
+a counting sort every `sort_every` steps): the large collisionless run,
+2048 x 2048 periodic cells, 32 electrons per cell (134,217,728 particles),
+Maxwellian vth = 0.05 with a density perturbation of amplitude 0.01 in mode
+(1,1), dt = 0.05, plasma units (eps0 = 1, omega_pe = 1), L = 2048 * 0.05.
+Data are synthetic (seeded Philox init).  The particle arrays (2.7 GB per
+pass) are far larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU step (the oracle's restatement of
+thesisCode/collisionless/double/src/{grid,fourier,particle}.cc, OpenMP on
+all host cores) on a bounded sample of the same workload.
+Under torchrun each rank runs an independent replica on its own GPU (a single
+run does not shard); value = all ranks' particle-steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "msc-thesis_gb300"))
+
+METRIC = "particle-steps/s per GB300 (plain vs batched+adjoint) at <=1e-5 rel err; % HBM"
+NX = NY = 2048
+PPC = 32
+N = NX * NY * PPC
+DX = 0.05
+L = NX * DX
+DT = 0.05
+VTH = 0.05
+SORT_EVERY = 20
+# algorithmic bytes: 40 per particle-step (20 B read + 20 B written: int32 cell,
+# 2 x fp32 offset, 2 x fp32 velocity) and 60 per cell-step (int64 density
+# write+read 16, R2C 8, k-space 12, 2 x C2R 16, field window read 8)
+BYTES_PER_PARTICLE = 40
+BYTES_PER_CELL = 60
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def launches_for(k, since_sort, S, nspecies=1):
+    """Our kernels launched by pic_step(k), following its schedule: per step
+    nspecies pushes + 2 advance + convert + kspace; per sort and species
+    histogram, 3 scan kernels and the scatter.  Returns (count, since_sort)."""
+    n, cnt = k, 0
+    while n > 0:
+        if since_sort >= S:
+            sorts, steps = 1, (S if n >= S else 1)
+            since_sort = steps
+        else:
+            sorts, steps = 0, 1
+            since_sort += 1
+        cnt += sorts * 5 * nspecies + steps * (nspecies + 4)
+        n -= steps
+    return cnt, since_sort
+
+
+def cpu_sample(nthreads):
+    """The reference's CPU step (oracle restatement, OpenMP) on a bounded
+    sample of the workload: 512 x 512 cells at 32 particles per cell."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle as O
+
+    p = O.ref_params(xDim=26, yDim=26, nx=512, ny=512, npx=4096, npy=2048, dt=DT, tmax=1.0,
+                     charge=-1.0, mass=1.0, vtx=VTH, vty=VTH)
+    x, y, vx, vy = O.compat_init(p, seed=1)
+    n = len(x)
+    return p, (x, y, vx, vy), n, f"512x512 cells, 32 ppc ({n} particles), reference conventions"
+
+
+def time_cpu(steps, nthreads):
+    import oracle as O
+
+    p, st, n, desc = cpu_sample(nthreads)
+    t0 = time.perf_counter()
+    O.compat_run(p, *st, steps, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return n * steps / dt, desc, n
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    if not os.path.exists(os.path.join(ROOT, "oracle", "build", "liboracle.so")):
+        O.build()
+    nthreads = os.cpu_count() or 1
+    p, st, n, desc = cpu_sample(nthreads)
+    O.compat_run(p, *st, max(1, args.warmup), nthreads=nthreads)
+    t0 = time.perf_counter()
+    O.compat_run(p, *st, args.steps, nthreads=nthreads)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"reference CPU step on a sample of landau-{NX}x{NY}-{PPC}ppc",
+                   "sample": desc},
+        "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": nthreads,
+                         "kind": "port", "sample": desc},
+        "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    import picgpu as P
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    A = L * L
+    sp = P.species(N, -A / N, A / N, -1)
+    cfg = P.config(NX, NY, L, L, DT, [sp], sort_every=SORT_EVERY, device=local)
+    h = P.Handle(cfg)
+    spec = P.init_spec(N, vth=(VTH, VTH, 0), pert_kind=P.PERT_DENSITY, pert_amp=0.01,
+                       pert_mx=1, pert_my=1, seed=2024 + rank)
+    h.init_particles(0, spec)
+    h.prime_leapfrog()
+    stream = torch.cuda.ExternalStream(h.stream())
+
+    # warm-up, then exactly K timed steps bracketed by barrier + synchronize
+    h.step(args.warmup)
+    h.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    h.step(args.steps)
+    e1.record(stream)
+    h.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    ms_max = ms
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * N * args.steps / (ms_max / 1000.0)
+    diag = h.diagnostics()
+
+    # dominant kernel (fused gather+push+deposit): eager launches timed with
+    # CUDA events on the handle's stream
+    reps = 5
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h.gather_push(True)
+    h.poisson()
+    p0.record(stream)
+    for _ in range(reps):
+        h.gather_push(True)
+    p1.record(stream)
+    h.synchronize()
+    push_ms = p0.elapsed_time(p1) / reps
+    h.poisson()
+    hbm, peak_kind = peaks()
+    achieved = BYTES_PER_PARTICLE * N / (push_ms / 1000.0) / 1e9
+    step_bytes = BYTES_PER_PARTICLE * N + BYTES_PER_CELL * NX * NY
+
+    # end to end through the C ABI from pinned host memory: copy in, K steps,
+    # copy out (pic_run_host)
+    e2e = None
+    if not args.no_e2e:
+        a = h.get_particles(0)
+        pin = lambda arr: torch.from_numpy(arr).pin_memory()
+        hin = [pin(a[k]) for k in ("x", "y", "vx", "vy")]
+        hout = [torch.empty(N, dtype=torch.float64).pin_memory() for _ in range(4)]
+        del a
+        barrier()
+        t0 = time.perf_counter()
+        h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.steps, 1,
+             *[x.data_ptr() for x in hout])
+        el = time.perf_counter() - t0
+        if pg:
+            t = torch.tensor([el], device="cuda")
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": world * N * args.steps / el, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 32 * N / args.steps, "d2h_bytes_per_step": 32 * N / args.steps,
+               "seconds": el, "steps": args.steps}
+        del hin, hout
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        nthreads = os.cpu_count() or 1
+        v, desc, _ = time_cpu(2, nthreads)
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
+               "sample": desc + ", 2 steps"}
+
+    _, since_after_warmup = launches_for(args.warmup, 0, SORT_EVERY)
+    launches, _ = launches_for(args.steps, since_after_warmup, SORT_EVERY)
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"landau-{NX}x{NY}-{PPC}ppc", "nx": NX, "ny": NY,
+                       "particles": N, "dt": DT, "sort_every": SORT_EVERY,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (2.7 GB particle arrays per step)",
+                       "hbm_frac_step": step_bytes * args.steps / (ms_max / 1000.0) / 1e9 / hbm,
+                       "peak_kind": peak_kind,
+                       "charge_exact": diag.total_charge_fixed == diag.expected_charge_fixed,
+                       "field_energy": diag.field_energy},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "kernel": "push_kernel (fused gather+push+deposit)",
+                         "kernel_ms": push_ms},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
+    h.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

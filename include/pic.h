@@ -1,0 +1,270 @@
+/*
+ * pic.h -- C ABI of libpic, a GB300-native (sm_103a) 2-D electrostatic
+ * particle-in-cell step: particle/grid init, charge deposit, Poisson solve,
+ * field gather + push, collisions and diagnostics.
+ *
+ * Every call returns a pic_status; nothing calls exit().  Pointers are plain
+ * host pointers unless a name says "_dev".  A handle owns its CUDA stream and
+ * all device buffers; one handle per host thread makes the library re-entrant.
+ *
+ * Reference interfaces replaced (paths inside taylorj5/msc-thesis,
+ * thesisCode/collisionless/double/ unless stated):
+ *   pic_compat_run        <- picFloatGpu              inc/pic.h:5-7, src/pic.cu:429-611
+ *   pic_compat_run_steps  <- the CPU step loop body   src/main.cc:137-172
+ *   pic_init_particles    <- initialiseParticles      src/main.cc:201-244
+ *   pic_set_particles     <- Particle::Particle       src/particle.cc:21-29
+ *   pic_deposit           <- Grid::chargeAssignment   src/grid.cc:46-76
+ *   pic_deposit_grid      <- Grid::chargeAssignment   src/grid.cc:46-76 (stateless form)
+ *   pic_poisson           <- fftPoissonSolver + Grid::computeElectricField
+ *                                                     src/fourier.cc:15-126, src/grid.cc:85-96
+ *   pic_gather_push       <- Particle::forceCalculation + Particle::positionUpdate
+ *                                                     src/particle.cc:37-106
+ *   pic_collide           <- Particle::collision (mccCollisions/src/particle.cc:112-127),
+ *                            collisions (dsmcCollisions/cellTrackerAdvanced/src/main.cc:288-350)
+ *   pic_sort              <- cellTracking (dsmcCollisions/cellTrackerAdvanced/src/main.cc:269-278)
+ *   pic_diagnostics       <- checkResults / checkError (src/main.cc:254-267;
+ *                            dsmcCollisions/cellTrackerAdvanced/src/main.cc:380-408)
+ *   pic_get_particles, pic_get_grid <- the D2H copies at src/pic.cu:583-584 and the
+ *                            public Grid arrays (inc/grid.h:27-29)
+ */
+#ifndef PIC_H
+#define PIC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* status                                                              */
+/* ------------------------------------------------------------------ */
+typedef enum pic_status {
+    PIC_OK = 0,
+    PIC_ERR_INVALID_ARG = 1, /* bad config or argument                     */
+    PIC_ERR_OOM = 2,         /* device or host allocation failed           */
+    PIC_ERR_CUDA = 3,        /* a CUDA runtime call failed                 */
+    PIC_ERR_CUFFT = 4,       /* a cuFFT call failed                        */
+    PIC_ERR_OVERFLOW = 5,    /* capacity exceeded (particles, cells)       */
+    PIC_ERR_NAN = 6,         /* non-finite particle state detected         */
+    PIC_ERR_TIMEOUT = 7,     /* a bounded device wait gave up              */
+    PIC_ERR_STATE = 8,       /* call not valid in the handle's state       */
+    PIC_ERR_NO_DEVICE = 9    /* no CUDA device visible                     */
+} pic_status;
+
+/* Static English text for a status. */
+const char *pic_status_string(pic_status s);
+/* Detail of the last failure on the calling thread ("" if none). */
+const char *pic_last_error(void);
+/* Library version, e.g. "1.0.0". */
+const char *pic_version(void);
+
+/* ------------------------------------------------------------------ */
+/* reference drop-in: the reference's conventions, FP64 on the GPU    */
+/* ------------------------------------------------------------------ */
+/* The fields of the reference's struct Params that its step reads
+ * (inc/params.h:21-47), as plain data.  xDim/yDim are int there too. */
+typedef struct pic_ref_params {
+    int xDim, yDim;      /* domain size                                   */
+    int nx, ny;          /* cells per direction                           */
+    int npx, npy;        /* particles = npx * npy                         */
+    double dt, tmax;     /* step count = iterations of while (t < tmax)   */
+    double charge, mass; /* macro-particle charge and mass                */
+    double vtx, vty, vdx, vdy;
+} pic_ref_params;
+
+/* Drop-in for picFloatGpu (inc/pic.h:6): copies the four initial particle
+ * arrays to the device, runs the reference's step (src/main.cc:137-172 with
+ * the CPU conventions of grid.cc, fourier.cc, particle.cc) for as many
+ * steps as `while (t < tmax) t += dt` iterates, and copies the final
+ * positions back.  *seconds (may be NULL) receives the elapsed time of the
+ * whole call, as picFloatGpu returns it.  Unlike picFloatGpu the deposit
+ * is atomic, the density is zeroed each step and forceOld starts at zero for
+ * every particle, so the result follows the reference's CPU path. */
+pic_status pic_compat_run(const pic_ref_params *p, const double *posX, const double *posY,
+                          const double *velX, const double *velY, double *xOut, double *yOut,
+                          double *seconds);
+
+/* Same step for an explicit number of steps, returning the final particle
+ * arrays and the ghost-padded (nx+2)*(ny+2) grids rho, phi, Ex, Ey (row
+ * index = x cell, as in the reference's Grid).  Any output may be NULL. */
+pic_status pic_compat_run_steps(const pic_ref_params *p, const double *x0, const double *y0,
+                                const double *vx0, const double *vy0, long long nsteps,
+                                double *x, double *y, double *vx, double *vy, double *rho,
+                                double *phi, double *ex, double *ey);
+
+/* ------------------------------------------------------------------ */
+/* physics-mode handle                                                 */
+/* ------------------------------------------------------------------ */
+#define PIC_MAX_SPECIES 4
+
+enum pic_species_flags {
+    PIC_SPECIES_HAS_VZ = 1 /* carry a third velocity component (collisions) */
+};
+
+typedef struct pic_species_desc {
+    long long capacity; /* maximum particle count held on the device           */
+    double q;           /* macro-particle charge (0 for a neutral species)     */
+    double m;           /* macro-particle mass                                 */
+    int q_int;          /* charge in deposit units: q = q_int * unit charge    */
+    int flags;          /* pic_species_flags                                   */
+} pic_species_desc;
+
+typedef struct pic_config {
+    int nx, ny;          /* cells; periodic in both directions                */
+    double Lx, Ly;       /* domain lengths                                    */
+    double dt;           /* time step                                         */
+    double eps0;         /* vacuum permittivity in the chosen units           */
+    int nspecies;
+    pic_species_desc species[PIC_MAX_SPECIES];
+    int sort_every;      /* steps between counting sorts (0: 20)              */
+    int tile_w, tile_h;  /* sort tile in cells (0: chosen from the density)   */
+    int chunk;           /* particles per push block, multiple of 4 (0: auto) */
+    int halo;            /* shared-memory window halo in cells (0: 2)         */
+    int history;         /* diagnostic history length in steps (0: 4096)      */
+    int device;          /* CUDA device ordinal                               */
+} pic_config;
+
+typedef struct pic_handle pic_handle;
+
+pic_status pic_config_default(pic_config *cfg);
+pic_status pic_create(const pic_config *cfg, pic_handle **out);
+pic_status pic_destroy(pic_handle *h);
+/* The CUDA stream all of the handle's work runs on (cudaStream_t). */
+pic_status pic_get_stream(pic_handle *h, void **stream);
+/* Wait for the handle's stream; reports device error flags. */
+pic_status pic_synchronize(pic_handle *h);
+
+enum pic_load { PIC_LOAD_RANDOM = 0, PIC_LOAD_LATTICE = 1 };
+enum pic_pert { PIC_PERT_NONE = 0, PIC_PERT_XDISP = 1, PIC_PERT_DENSITY = 2 };
+
+typedef struct pic_init_spec {
+    long long n;        /* particles to create                                */
+    int layout;         /* pic_load                                           */
+    int pert_kind;      /* pic_pert                                           */
+    double vth[3];      /* thermal speeds (Gaussian sigma) per component      */
+    double vdrift[2];   /* drift velocity                                     */
+    double beam_v;      /* != 0: two beams, +beam_v (even id) / -beam_v (odd) */
+    double pert_amp;    /* XDISP: x += amp cos(kx x); DENSITY: n ~ 1+amp cos(k.x) */
+    int pert_mx, pert_my; /* perturbation mode numbers (k = 2 pi m / L)       */
+    unsigned long long seed;
+} pic_init_spec;
+
+/* Create spec->n particles of a species on the device (Philox streams keyed
+ * by seed and particle id), sort them, deposit and solve for E. */
+pic_status pic_init_particles(pic_handle *h, int species, const pic_init_spec *spec);
+/* Replace a species' particles from host arrays: positions in [0, L)
+ * (global coordinates), velocities; vz may be NULL.  Particle ids are the
+ * array indices.  Sorts, deposits and solves for E afterwards. */
+pic_status pic_set_particles(pic_handle *h, int species, long long n, const double *x,
+                             const double *y, const double *vx, const double *vy,
+                             const double *vz);
+/* Copy a species to host arrays in particle-id order (id i -> index i).
+ * *n receives the count; any array may be NULL. */
+pic_status pic_get_particles(pic_handle *h, int species, long long *n, double *x, double *y,
+                             double *vx, double *vy, double *vz);
+
+/* Copy a species' raw device storage to host arrays in storage order (the
+ * sorted order, not id order); any array may be NULL. */
+pic_status pic_get_particles_raw(pic_handle *h, int species, long long *n, int32_t *cell,
+                                 float *ox, float *oy, float *vx, float *vy, uint32_t *pid);
+
+/* Borrowed device views of a species' SoA storage (valid until the next
+ * call that sorts or resizes): cell = cx | (cy << 16) (int32), in-cell
+ * offsets ox, oy in [0,1) (float), velocities (float), particle id (uint32). */
+typedef struct pic_particles_view {
+    long long n;
+    int32_t *cell_dev;
+    float *ox_dev, *oy_dev, *vx_dev, *vy_dev, *vz_dev;
+    uint32_t *pid_dev;
+} pic_particles_view;
+pic_status pic_particles_device(pic_handle *h, int species, pic_particles_view *v);
+
+/* Time-leapfrog priming: v <- v - (q/m) E(x) dt/2 for every charged
+ * species, using the current field. */
+pic_status pic_prime_leapfrog(pic_handle *h);
+
+/* ---- the step stages ---- */
+pic_status pic_sort(pic_handle *h);    /* counting sort of every species by cell tile */
+pic_status pic_deposit(pic_handle *h); /* fixed-point rho from the current positions  */
+pic_status pic_poisson(pic_handle *h); /* rho -> E (cuFFT R2C, k-space kernel, C2R)   */
+/* Gather E, push every species one step; with deposit != 0 the new charge
+ * density is deposited in the same pass (then pic_poisson gives E). */
+pic_status pic_gather_push(pic_handle *h, int deposit);
+
+enum pic_collide_kind { PIC_COLLIDE_MCC = 1, PIC_COLLIDE_DSMC = 2 };
+pic_status pic_collide(pic_handle *h, int kind);
+
+/* nsteps full steps (push+deposit, Poisson, sort every sort_every), replayed
+ * from CUDA graphs.  Asynchronous: returns once the work is queued. */
+pic_status pic_step(pic_handle *h, long long nsteps);
+
+/* Whole run from and to host memory through one call, as the reference's
+ * GPU driver is used: copy species 0 in (global coordinates), deposit,
+ * solve, prime the leapfrog when prime != 0, step nsteps times and copy the
+ * final state back (in id order).  Outputs may alias inputs. */
+pic_status pic_run_host(pic_handle *h, long long n, const double *x, const double *y,
+                        const double *vx, const double *vy, long long nsteps, int prime,
+                        double *x_out, double *y_out, double *vx_out, double *vy_out);
+
+/* ---- diagnostics ---- */
+typedef struct pic_diag {
+    long long step;              /* completed steps                           */
+    double field_energy;         /* 1/2 eps0 sum |E|^2 dA at `step`           */
+    double kinetic_energy;       /* at step-1 (time-centred), all species     */
+    double momentum[2];          /* at step-1, all species                    */
+    long long total_charge_fixed; /* sum of the fixed-point density (2^-32 q units) */
+    long long expected_charge_fixed; /* sum over species of q_int * n * 2^32  */
+    long long n[PIC_MAX_SPECIES];
+    unsigned int error_flags;    /* PIC_DEVERR_* bits                         */
+} pic_diag;
+
+enum pic_device_errors {
+    PIC_DEVERR_NAN = 1,       /* a particle had a non-finite velocity          */
+    PIC_DEVERR_CAPACITY = 2,  /* a species ran out of capacity (ionisation)    */
+    PIC_DEVERR_CELL = 4       /* a cell index outside the grid was seen        */
+};
+
+pic_status pic_diagnostics(pic_handle *h, pic_diag *d);
+
+enum pic_history {
+    PIC_HIST_FIELD_ENERGY = 0, /* indexed by step (0 = initial field)          */
+    PIC_HIST_KINETIC = 1,      /* indexed by step of the push                  */
+    PIC_HIST_MOMENTUM_X = 2,
+    PIC_HIST_MOMENTUM_Y = 3,
+    PIC_HIST_CHARGE = 4,       /* total fixed-point charge, as a double        */
+    PIC_HIST_MODE_AMP = 5      /* |rho^(mx,my)| of the tracked mode (pic_track_mode) */
+};
+/* Copy history entries [first, first+count) (steps) to host. */
+pic_status pic_get_history(pic_handle *h, int which, long long first, long long count,
+                           double *out);
+/* Track |rho^| of one Fourier mode each step (PIC_HIST_MODE_AMP). */
+pic_status pic_track_mode(pic_handle *h, int mx, int my);
+
+enum pic_grid_kind { PIC_GRID_RHO = 0, PIC_GRID_PHI = 1, PIC_GRID_EX = 2, PIC_GRID_EY = 3 };
+/* Copy a grid (row-major [iy][ix], nx*ny doubles) to host.  RHO is the net
+ * charge density of the last field solve, i.e. the particles' density plus
+ * the uniform neutralising background (its mean is zero); PHI is computed
+ * on request from that density. */
+pic_status pic_get_grid(pic_handle *h, int which, double *out);
+/* The raw fixed-point density of the last deposit (int64, 2^-32 charge
+ * units, before the background is removed). */
+pic_status pic_get_rho_fixed(pic_handle *h, int64_t *out);
+
+/* ------------------------------------------------------------------ */
+/* stateless deposit of device particle arrays                         */
+/* ------------------------------------------------------------------ */
+/* CIC deposit of n particles (cell = cx | (cy << 16), offsets in [0,1))
+ * into rho_dev (nx*ny doubles, row-major [iy][ix]), which is overwritten
+ * with q_int * scale * (fixed-point density / 2^32).  Accumulates in an
+ * int64 scratch grid that this call allocates on the device and frees.
+ * stream may be NULL (legacy default stream).  Entries with cell < 0 are
+ * skipped. */
+pic_status pic_deposit_grid(int nx, int ny, long long n, const int32_t *cell_dev,
+                            const float *ox_dev, const float *oy_dev, int q_int, double scale,
+                            double *rho_dev, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIC_H */

@@ -1,0 +1,230 @@
+// pic_init.cu -- creating, importing and exporting particles.
+//
+// Replaces (taylorj5/msc-thesis, thesisCode/collisionless/double/src/):
+//   main.cc:201-244     initialiseParticles (lattice + Gaussian + drift)
+//   particle.cc:21-29   Particle::Particle  (cell from position)
+//   pic.cu:520-523, 583-584  the host<->device particle copies
+// Random numbers come from Philox4x32-10 keyed by (seed) with the counter
+// (particle id, block, 0, STREAM_INIT), so every particle's initial state
+// depends only on the seed and its id.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pic_internal.cuh"
+
+namespace pic {
+
+struct InitArgs {
+    int32_t *cell;
+    float *ox, *oy, *vx, *vy, *vz;
+    uint32_t *pid;
+    long long n;
+    int nx, ny;
+    double Lx, Ly, dx, dy;
+    int layout, pert_kind, lat_nx, lat_ny;
+    double vth0, vth1, vth2, vd0, vd1, beam_v, amp;
+    double kx, ky;  // perturbation wavevector
+    uint32_t k0, k1;
+};
+
+// global position -> (cell, offset) with periodic wrap
+__device__ __forceinline__ void locate(double x, double L, double d, int n, int &c, float &o)
+{
+    x -= L * floor(x / L);
+    double g = x / d;
+    double f = floor(g);
+    int i = (int)f;
+    float fr = (float)(g - f);
+    if (fr >= 1.0f) {
+        fr = 0.0f;
+        i += 1;
+    }
+    if (i >= n) i -= n;
+    if (i < 0) i += n;
+    c = i;
+    o = fr;
+}
+
+__global__ void __launch_bounds__(256) init_kernel(InitArgs A)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += stride) {
+        const U4 r0 = philox4x32_10(U4{(uint32_t)i, (uint32_t)(i >> 32), 0u, STREAM_INIT}, A.k0, A.k1);
+        const U4 r1 = philox4x32_10(U4{(uint32_t)i, (uint32_t)(i >> 32), 1u, STREAM_INIT}, A.k0, A.k1);
+        double x, y;
+        if (A.layout == PIC_LOAD_LATTICE) {
+            const long long ix = i % A.lat_nx, iy = i / A.lat_nx;
+            x = ((double)ix + 0.5) * (A.Lx / A.lat_nx);
+            y = ((double)iy + 0.5) * (A.Ly / A.lat_ny);
+        } else {
+            x = u01d(r0.x) * A.Lx;
+            y = u01d(r0.y) * A.Ly;
+        }
+        if (A.pert_kind == PIC_PERT_XDISP) {
+            x += A.amp * cos(A.kx * x);
+        } else if (A.pert_kind == PIC_PERT_DENSITY) {
+            // displacement -(amp/|k|^2) k sin(k.x) gives n ~ 1 + amp cos(k.x) to first order
+            const double k2 = A.kx * A.kx + A.ky * A.ky;
+            const double s = sin(A.kx * x + A.ky * y) * (A.amp / k2);
+            x -= A.kx * s;
+            y -= A.ky * s;
+        }
+        int cx, cy;
+        float ox, oy;
+        locate(x, A.Lx, A.dx, A.nx, cx, ox);
+        locate(y, A.Ly, A.dy, A.ny, cy, oy);
+        // Box-Muller normals
+        const float ra = sqrtf(-2.f * logf(u01f(r0.z)));
+        float sa, ca;
+        sincospif(2.f * u01f(r0.w), &sa, &ca);
+        const float rb = sqrtf(-2.f * logf(u01f(r1.x)));
+        float sb, cb;
+        sincospif(2.f * u01f(r1.y), &sb, &cb);
+        double vx = A.vd0 + A.vth0 * (double)(ra * ca);
+        const double vy = A.vd1 + A.vth1 * (double)(ra * sa);
+        if (A.beam_v != 0.0) vx += (i & 1) ? -A.beam_v : A.beam_v;
+        A.cell[i] = cx | (cy << 16);
+        A.ox[i] = ox;
+        A.oy[i] = oy;
+        A.vx[i] = (float)vx;
+        A.vy[i] = (float)vy;
+        if (A.vz) A.vz[i] = (float)(A.vth2 * (double)(rb * cb));
+        A.pid[i] = (uint32_t)i;
+    }
+}
+
+__global__ void from_global_kernel(InitArgs A, const double *x, const double *y, const double *vx,
+                                   const double *vy, const double *vz)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += stride) {
+        int cx, cy;
+        float ox, oy;
+        locate(x[i], A.Lx, A.dx, A.nx, cx, ox);
+        locate(y[i], A.Ly, A.dy, A.ny, cy, oy);
+        A.cell[i] = cx | (cy << 16);
+        A.ox[i] = ox;
+        A.oy[i] = oy;
+        A.vx[i] = (float)vx[i];
+        A.vy[i] = (float)vy[i];
+        if (A.vz) A.vz[i] = vz ? (float)vz[i] : 0.f;
+        A.pid[i] = (uint32_t)i;
+    }
+}
+
+// Export in id order: out[pid[i]] = particle i.
+__global__ void to_global_kernel(const int32_t *cell, const float *ox, const float *oy,
+                                 const float *vx, const float *vy, const float *vz,
+                                 const uint32_t *pid, const long long *d_n, double dx, double dy,
+                                 double *x, double *y, double *ux, double *uy, double *uz)
+{
+    const long long n = *d_n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t p = pid[i];
+        if ((long long)p >= n) continue;
+        const int c = cell[i];
+        const int cx = c & 0xFFFF, cy = c >> 16;
+        if (x) x[p] = ((double)cx + (double)ox[i]) * dx;
+        if (y) y[p] = ((double)cy + (double)oy[i]) * dy;
+        if (ux) ux[p] = vx[i];
+        if (uy) uy[p] = vy[i];
+        if (uz) uz[p] = vz ? (double)vz[i] : 0.0;
+    }
+}
+
+__global__ void fill_padding_kernel(int32_t *c0, int32_t *c1, long long from, long long to)
+{
+    const long long i = from + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < to) {
+        c0[i] = -1;
+        c1[i] = -1;
+    }
+}
+
+static InitArgs base_args(pic_handle *h, int s)
+{
+    SpeciesBuf &B = h->sp[s];
+    const Geometry &g = h->g;
+    InitArgs A;
+    memset(&A, 0, sizeof(A));
+    A.cell = B.cell[0];
+    A.ox = B.ox[0];
+    A.oy = B.oy[0];
+    A.vx = B.vx[0];
+    A.vy = B.vy[0];
+    A.vz = B.vz[0];
+    A.pid = B.pid[0];
+    A.nx = g.nx;
+    A.ny = g.ny;
+    A.Lx = g.Lx;
+    A.Ly = g.Ly;
+    A.dx = g.dx;
+    A.dy = g.dy;
+    return A;
+}
+
+pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_nx, int lat_ny)
+{
+    InitArgs A = base_args(h, s);
+    A.n = spec->n;
+    A.layout = spec->layout;
+    A.pert_kind = spec->pert_kind;
+    A.lat_nx = lat_nx;
+    A.lat_ny = lat_ny;
+    A.vth0 = spec->vth[0];
+    A.vth1 = spec->vth[1];
+    A.vth2 = spec->vth[2];
+    A.vd0 = spec->vdrift[0];
+    A.vd1 = spec->vdrift[1];
+    A.beam_v = spec->beam_v;
+    A.amp = spec->pert_amp;
+    A.kx = 2.0 * 3.14159265358979323846 * spec->pert_mx / h->g.Lx;
+    A.ky = 2.0 * 3.14159265358979323846 * spec->pert_my / h->g.Ly;
+    A.k0 = (uint32_t)spec->seed;
+    A.k1 = (uint32_t)(spec->seed >> 32);
+    if (A.n > 0) {
+        init_kernel<<<grid_for(A.n, 256), 256, 0, h->stream>>>(A);
+        PIC_CUDA(cudaGetLastError());
+    }
+    return PIC_OK;
+}
+
+pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x_dev,
+                              const double *y_dev, const double *vx_dev, const double *vy_dev,
+                              const double *vz_dev)
+{
+    InitArgs A = base_args(h, s);
+    A.n = n;
+    if (n > 0) {
+        from_global_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(A, x_dev, y_dev, vx_dev, vy_dev,
+                                                                  vz_dev);
+        PIC_CUDA(cudaGetLastError());
+    }
+    return PIC_OK;
+}
+
+pic_status launch_to_global(pic_handle *h, int s, double *x_dev, double *y_dev, double *vx_dev,
+                            double *vy_dev, double *vz_dev)
+{
+    SpeciesBuf &B = h->sp[s];
+    if (B.cap == 0) return PIC_OK;
+    to_global_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(
+        B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.vz[0], B.pid[0], &h->dev->n[s], h->g.dx,
+        h->g.dy, x_dev, y_dev, vx_dev, vy_dev, vz_dev);
+    PIC_CUDA(cudaGetLastError());
+    return PIC_OK;
+}
+
+pic_status launch_fill_padding(pic_handle *h, int s, long long from, long long to)
+{
+    SpeciesBuf &B = h->sp[s];
+    if (to <= from) return PIC_OK;
+    const long long m = to - from;
+    fill_padding_kernel<<<(unsigned)((m + 255) / 256), 256, 0, h->stream>>>(B.cell[0], B.cell[1],
+                                                                          from, to);
+    PIC_CUDA(cudaGetLastError());
+    return PIC_OK;
+}
+
+}  // namespace pic

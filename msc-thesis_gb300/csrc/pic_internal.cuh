@@ -1,0 +1,178 @@
+// pic_internal.cuh -- shared declarations of libpic's translation units.
+//
+// Device data layout (physics mode), per species, structure of arrays:
+//   cell  int32  cx | (cy << 16); -1 marks an empty (padding) slot
+//   ox,oy float  in-cell offsets in [0,1), in cell units
+//   vx,vy float  velocity (vz when PIC_SPECIES_HAS_VZ)
+//   pid   uint32 particle id (moved only by the sort)
+// Two copies (buffer 0 = live, buffer 1 = sort target).  Grids are row-major
+// [iy][ix]: the fixed-point density rho_fix (uint64, two's complement,
+// 2^-32 charge units), the float density rho (background removed), and the
+// field planes e[0] = Ex, e[1] = Ey.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "pic.h"
+
+namespace pic {
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string &msg);
+pic_status cuda_fail(cudaError_t e, const char *what);
+pic_status cufft_fail(cufftResult r, const char *what);
+
+#define PIC_CUDA(call)                                                                         \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) return ::pic::cuda_fail(e_, #call);                             \
+    } while (0)
+#define PIC_CUFFT(call)                                                                        \
+    do {                                                                                       \
+        cufftResult r_ = (call);                                                               \
+        if (r_ != CUFFT_SUCCESS) return ::pic::cufft_fail(r_, #call);                          \
+    } while (0)
+#define PIC_TRY(call)                                                                          \
+    do {                                                                                       \
+        pic_status s_ = (call);                                                                \
+        if (s_ != PIC_OK) return s_;                                                           \
+    } while (0)
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon et al., SC'11): published multipliers and Weyl
+// key increments; 10 rounds.
+struct U4 {
+    uint32_t x, y, z, w;
+};
+__host__ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    }
+    return c;
+}
+// (0,1) open interval from 32 random bits
+__host__ __device__ __forceinline__ float u01f(uint32_t r)
+{
+    return ((float)(r >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+__host__ __device__ __forceinline__ double u01d(uint32_t r)
+{
+    return ((double)r + 0.5) * (1.0 / 4294967296.0);
+}
+
+// Philox stream identifiers (counter word 3)
+enum : uint32_t {
+    STREAM_INIT = 0x696e6974u,   // "init"
+    STREAM_MCC = 0x6d636321u,    // "mcc!"
+    STREAM_DSMC = 0x64736d63u    // "dsmc"
+};
+
+// ------------------------------------------------------------------ handle
+struct SpeciesBuf {
+    int32_t *cell[2] = {nullptr, nullptr};
+    float *ox[2] = {nullptr, nullptr}, *oy[2] = {nullptr, nullptr};
+    float *vx[2] = {nullptr, nullptr}, *vy[2] = {nullptr, nullptr};
+    float *vz[2] = {nullptr, nullptr};
+    uint32_t *pid[2] = {nullptr, nullptr};
+    int32_t *anchor = nullptr;  // per push chunk: tile (tx | ty << 16) or -1
+    long long cap = 0;          // allocated slots (multiple of 4)
+    long long n = 0;            // host mirror of the count
+    long long nchunks = 0;      // push grid size for this species
+};
+
+// Device-side accumulators and counters (one struct in device memory).
+struct DevState {
+    double ke, px, py;        // accumulated by the push of the current step
+    double fe;                // accumulated by the k-space kernel
+    double mode_amp;          // |rho^| of the tracked mode
+    unsigned long long q;     // sum of the fixed-point density (convert kernel)
+    long long step;           // completed steps
+    long long n[PIC_MAX_SPECIES];
+    unsigned int err;         // PIC_DEVERR_* bits
+    unsigned int pad;
+};
+
+struct Geometry {
+    int nx, ny, nh;           // nh = nx/2 + 1 (half spectrum along x)
+    double Lx, Ly, dx, dy;
+    int tw, th, ntx, nty;     // sort tiles
+    int halo, chunk;
+    int wcx, wcy;             // cell window of a push block: (2 tw + 2 halo) x (th + 2 halo)
+};
+
+}  // namespace pic
+
+struct pic_handle {
+    pic_config cfg;
+    pic::Geometry g;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    pic::SpeciesBuf sp[PIC_MAX_SPECIES];
+    double q_unit = 0.0;       // charge of one deposit unit (q = q_int * q_unit)
+    long long mean_fix = 0;    // background: mean fixed-point density per node
+    // grids
+    unsigned long long *rho_fix = nullptr;  // nx*ny
+    float *rho = nullptr;                    // nx*ny
+    float2 *rhohat = nullptr;                // ny*nh
+    float2 *ehat = nullptr;                  // 2*ny*nh
+    float *e = nullptr;                      // 2*nx*ny: Ex plane then Ey plane
+    cufftHandle plan_r2c = 0, plan_c2r2 = 0, plan_c2r1 = 0;
+    // sort
+    uint32_t *count = nullptr, *offset = nullptr, *cursor = nullptr, *bsum = nullptr;
+    int scan_blocks = 0;
+    // diagnostics
+    pic::DevState *dev = nullptr;
+    double *hist = nullptr;  // 6 * hist_cap doubles, see pic_history
+    int hist_cap = 0;
+    int track_mx = -1, track_my = -1;
+    // graphs
+    cudaGraphExec_t g_period = nullptr, g_sortstep = nullptr, g_one = nullptr;
+    int since_sort = 0;
+    bool graphs_valid = false;
+    bool fields_valid = false;
+    long long steps_host = 0;
+    // host<->device staging for imports and exports (grown on demand)
+    void *stage = nullptr;
+    size_t stage_bytes = 0;
+};
+
+namespace pic {
+
+// ------------------------------------------------------------------ launchers
+// pic_push.cu
+pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale);
+pic_status launch_deposit(pic_handle *h, int s);
+// pic_field.cu
+pic_status launch_convert(pic_handle *h);
+pic_status launch_kspace(pic_handle *h, bool phi_only, float2 *phihat);
+enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
+pic_status launch_advance(pic_handle *h, int kind);
+// pic_sort.cu
+pic_status launch_sort(pic_handle *h, int s);
+// pic_init.cu
+pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_nx, int lat_ny);
+pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x_dev,
+                              const double *y_dev, const double *vx_dev, const double *vy_dev,
+                              const double *vz_dev);
+pic_status launch_to_global(pic_handle *h, int s, double *x_dev, double *y_dev, double *vx_dev,
+                            double *vy_dev, double *vz_dev);
+pic_status launch_fill_padding(pic_handle *h, int s, long long from, long long to);
+
+// grid-stride launch size for `n` items on the current device
+int grid_for(long long n, int block);
+
+}  // namespace pic

@@ -1,0 +1,355 @@
+"""Python binding of libpic's C ABI (include/pic.h) through ctypes.
+
+This is the host-side mirror of the reference's step interface
+(taylorj5/msc-thesis thesisCode/collisionless/double/src/main.cc:137-172):
+``Handle.init_particles`` / ``set_particles`` (initialiseParticles,
+Particle::Particle), ``deposit`` (Grid::chargeAssignment), ``poisson``
+(fftPoissonSolver + Grid::computeElectricField), ``gather_push``
+(Particle::forceCalculation + positionUpdate), ``collide``, ``step`` and
+``diagnostics``; ``compat_run`` is the drop-in for picFloatGpu.
+
+Every failing call raises ``PicError`` with the library's status and message.
+There is no fallback: if libpic.so is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpic.so")
+
+MAX_SPECIES = 4
+SPECIES_HAS_VZ = 1
+LOAD_RANDOM, LOAD_LATTICE = 0, 1
+PERT_NONE, PERT_XDISP, PERT_DENSITY = 0, 1, 2
+COLLIDE_MCC, COLLIDE_DSMC = 1, 2
+GRID_RHO, GRID_PHI, GRID_EX, GRID_EY = 0, 1, 2, 3
+HIST_FIELD_ENERGY, HIST_KINETIC, HIST_MOMENTUM_X, HIST_MOMENTUM_Y, HIST_CHARGE, HIST_MODE_AMP = range(6)
+DEVERR_NAN, DEVERR_CAPACITY, DEVERR_CELL = 1, 2, 4
+
+STATUS = {0: "PIC_OK", 1: "PIC_ERR_INVALID_ARG", 2: "PIC_ERR_OOM", 3: "PIC_ERR_CUDA",
+          4: "PIC_ERR_CUFFT", 5: "PIC_ERR_OVERFLOW", 6: "PIC_ERR_NAN", 7: "PIC_ERR_TIMEOUT",
+          8: "PIC_ERR_STATE", 9: "PIC_ERR_NO_DEVICE"}
+
+
+class PicError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class RefParams(C.Structure):
+    """pic_ref_params: the reference's Params fields (inc/params.h:21-47)."""
+
+    _fields_ = [("xDim", C.c_int), ("yDim", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+                ("npx", C.c_int), ("npy", C.c_int), ("dt", C.c_double), ("tmax", C.c_double),
+                ("charge", C.c_double), ("mass", C.c_double), ("vtx", C.c_double),
+                ("vty", C.c_double), ("vdx", C.c_double), ("vdy", C.c_double)]
+
+
+class SpeciesDesc(C.Structure):
+    _fields_ = [("capacity", C.c_longlong), ("q", C.c_double), ("m", C.c_double),
+                ("q_int", C.c_int), ("flags", C.c_int)]
+
+
+class Config(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("Lx", C.c_double), ("Ly", C.c_double),
+                ("dt", C.c_double), ("eps0", C.c_double), ("nspecies", C.c_int),
+                ("species", SpeciesDesc * MAX_SPECIES), ("sort_every", C.c_int),
+                ("tile_w", C.c_int), ("tile_h", C.c_int), ("chunk", C.c_int), ("halo", C.c_int),
+                ("history", C.c_int), ("device", C.c_int)]
+
+
+class InitSpec(C.Structure):
+    _fields_ = [("n", C.c_longlong), ("layout", C.c_int), ("pert_kind", C.c_int),
+                ("vth", C.c_double * 3), ("vdrift", C.c_double * 2), ("beam_v", C.c_double),
+                ("pert_amp", C.c_double), ("pert_mx", C.c_int), ("pert_my", C.c_int),
+                ("seed", C.c_ulonglong)]
+
+
+class Diag(C.Structure):
+    _fields_ = [("step", C.c_longlong), ("field_energy", C.c_double),
+                ("kinetic_energy", C.c_double), ("momentum", C.c_double * 2),
+                ("total_charge_fixed", C.c_longlong), ("expected_charge_fixed", C.c_longlong),
+                ("n", C.c_longlong * MAX_SPECIES), ("error_flags", C.c_uint)]
+
+
+class ParticlesView(C.Structure):
+    _fields_ = [("n", C.c_longlong), ("cell_dev", C.c_void_p), ("ox_dev", C.c_void_p),
+                ("oy_dev", C.c_void_p), ("vx_dev", C.c_void_p), ("vy_dev", C.c_void_p),
+                ("vz_dev", C.c_void_p), ("pid_dev", C.c_void_p)]
+
+
+_dp = C.POINTER(C.c_double)
+_vp = C.c_void_p
+_H = C.c_void_p
+
+# name -> argtypes (restype is pic_status / int unless listed in _RESTYPES)
+SIGNATURES = {
+    "pic_status_string": [C.c_int],
+    "pic_last_error": [],
+    "pic_version": [],
+    "pic_compat_run": [C.POINTER(RefParams), _dp, _dp, _dp, _dp, _dp, _dp, _dp],
+    "pic_compat_run_steps": [C.POINTER(RefParams), _dp, _dp, _dp, _dp, C.c_longlong,
+                             _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp],
+    "pic_config_default": [C.POINTER(Config)],
+    "pic_create": [C.POINTER(Config), C.POINTER(_H)],
+    "pic_destroy": [_H],
+    "pic_get_stream": [_H, C.POINTER(_vp)],
+    "pic_synchronize": [_H],
+    "pic_init_particles": [_H, C.c_int, C.POINTER(InitSpec)],
+    "pic_set_particles": [_H, C.c_int, C.c_longlong, _vp, _vp, _vp, _vp, _vp],
+    "pic_get_particles": [_H, C.c_int, C.POINTER(C.c_longlong), _vp, _vp, _vp, _vp, _vp],
+    "pic_get_particles_raw": [_H, C.c_int, C.POINTER(C.c_longlong), _vp, _vp, _vp, _vp, _vp, _vp],
+    "pic_particles_device": [_H, C.c_int, C.POINTER(ParticlesView)],
+    "pic_prime_leapfrog": [_H],
+    "pic_sort": [_H],
+    "pic_deposit": [_H],
+    "pic_poisson": [_H],
+    "pic_gather_push": [_H, C.c_int],
+    "pic_collide": [_H, C.c_int],
+    "pic_step": [_H, C.c_longlong],
+    "pic_run_host": [_H, C.c_longlong, _vp, _vp, _vp, _vp, C.c_longlong, C.c_int,
+                     _vp, _vp, _vp, _vp],
+    "pic_diagnostics": [_H, C.POINTER(Diag)],
+    "pic_get_history": [_H, C.c_int, C.c_longlong, C.c_longlong, _vp],
+    "pic_track_mode": [_H, C.c_int, C.c_int],
+    "pic_get_grid": [_H, C.c_int, _vp],
+    "pic_get_rho_fixed": [_H, _vp],
+    "pic_deposit_grid": [C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp, C.c_int, C.c_double,
+                         _vp, _vp],
+}
+_RESTYPES = {"pic_status_string": C.c_char_p, "pic_last_error": C.c_char_p,
+             "pic_version": C.c_char_p}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libpic.so (raises OSError if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise OSError(f"libpic.so not built at {path}; run msc-thesis_gb300/build_lib.py")
+        L = C.CDLL(path)
+        for name, args in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _RESTYPES.get(name, C.c_int)
+        _lib = L
+    return _lib
+
+
+def _check(status: int, where: str):
+    if status != 0:
+        msg = load().pic_last_error().decode(errors="replace")
+        raise PicError(status, where, msg)
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ------------------------------------------------------------ compat ----
+def ref_params(**kw) -> RefParams:
+    """Defaults are the reference's struct Params defaults (params.h:22-42)."""
+    d = dict(xDim=10, yDim=10, nx=32, ny=32, npx=10, npy=10, dt=1e-7, tmax=1e-4,
+             charge=-100.0, mass=100.0, vtx=1.0, vty=1.0, vdx=0.0, vdy=0.0)
+    d.update(kw)
+    return RefParams(**d)
+
+
+def compat_run(p: RefParams, x, y, vx, vy):
+    """picFloatGpu drop-in: returns (xOut, yOut, seconds)."""
+    x, y, vx, vy = (_f64(a) for a in (x, y, vx, vy))
+    n = p.npx * p.npy
+    xo, yo = np.empty(n), np.empty(n)
+    sec = C.c_double(0)
+    dp = lambda a: a.ctypes.data_as(_dp)
+    _check(load().pic_compat_run(C.byref(p), dp(x), dp(y), dp(vx), dp(vy), dp(xo), dp(yo),
+                                 C.byref(sec)), "pic_compat_run")
+    return xo, yo, sec.value
+
+
+def compat_run_steps(p: RefParams, x, y, vx, vy, nsteps: int):
+    x, y, vx, vy = (_f64(a) for a in (x, y, vx, vy))
+    n = p.npx * p.npy
+    out = {k: np.empty(n) for k in ("x", "y", "vx", "vy")}
+    g = (p.nx + 2, p.ny + 2)
+    out.update({k: np.empty(g) for k in ("rho", "phi", "ex", "ey")})
+    dp = lambda a: a.ctypes.data_as(_dp)
+    _check(load().pic_compat_run_steps(C.byref(p), dp(x), dp(y), dp(vx), dp(vy), nsteps,
+                                       *[dp(out[k]) for k in ("x", "y", "vx", "vy", "rho",
+                                                             "phi", "ex", "ey")]),
+           "pic_compat_run_steps")
+    return out
+
+
+def deposit_grid(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale, rho_ptr, stream=None):
+    """Stateless deposit of device arrays (integer device pointers)."""
+    _check(load().pic_deposit_grid(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale, rho_ptr,
+                                   stream), "pic_deposit_grid")
+
+
+# ------------------------------------------------------------ handle ----
+def species(capacity, q, m, q_int, flags=0) -> SpeciesDesc:
+    return SpeciesDesc(int(capacity), float(q), float(m), int(q_int), int(flags))
+
+
+def config(nx, ny, Lx, Ly, dt, species_list, eps0=1.0, **tuning) -> Config:
+    c = Config()
+    _check(load().pic_config_default(C.byref(c)), "pic_config_default")
+    c.nx, c.ny, c.Lx, c.Ly, c.dt, c.eps0 = nx, ny, Lx, Ly, dt, eps0
+    c.nspecies = len(species_list)
+    for i, s in enumerate(species_list):
+        c.species[i] = s
+    for k, v in tuning.items():
+        setattr(c, k, v)
+    return c
+
+
+def init_spec(n, layout=LOAD_RANDOM, vth=(0.0, 0.0, 0.0), vdrift=(0.0, 0.0), beam_v=0.0,
+              pert_kind=PERT_NONE, pert_amp=0.0, pert_mx=0, pert_my=0, seed=0) -> InitSpec:
+    s = InitSpec()
+    s.n, s.layout, s.pert_kind = int(n), layout, pert_kind
+    for i in range(3):
+        s.vth[i] = float(vth[i]) if i < len(vth) else 0.0
+    s.vdrift[0], s.vdrift[1] = float(vdrift[0]), float(vdrift[1])
+    s.beam_v, s.pert_amp, s.pert_mx, s.pert_my, s.seed = beam_v, pert_amp, pert_mx, pert_my, seed
+    return s
+
+
+class Handle:
+    """One simulation on one GPU (owns a CUDA stream and its device buffers)."""
+
+    def __init__(self, cfg: Config):
+        self.cfg = cfg
+        h = C.c_void_p()
+        _check(load().pic_create(C.byref(cfg), C.byref(h)), "pic_create")
+        self.h = h
+        self.ncell = cfg.nx * cfg.ny
+
+    def close(self):
+        if self.h:
+            load().pic_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, name, *args):
+        _check(getattr(load(), name)(self.h, *args), name)
+
+    # ---- particles
+    def init_particles(self, s: int, spec: InitSpec):
+        self._c("pic_init_particles", s, C.byref(spec))
+
+    def set_particles(self, s, x, y, vx, vy, vz=None):
+        x, y, vx, vy = (_f64(a) for a in (x, y, vx, vy))
+        vz = None if vz is None else _f64(vz)
+        self._keep = (x, y, vx, vy, vz)
+        self._c("pic_set_particles", s, len(x), _ptr(x), _ptr(y), _ptr(vx), _ptr(vy), _ptr(vz))
+
+    def get_particles(self, s=0, vz=False):
+        n = C.c_longlong()
+        self._c("pic_get_particles", s, C.byref(n), None, None, None, None, None)
+        a = {k: np.empty(n.value) for k in ("x", "y", "vx", "vy")}
+        if vz:
+            a["vz"] = np.empty(n.value)
+        self._c("pic_get_particles", s, C.byref(n), _ptr(a["x"]), _ptr(a["y"]), _ptr(a["vx"]),
+                _ptr(a["vy"]), _ptr(a.get("vz")))
+        return a
+
+    def get_particles_raw(self, s=0):
+        n = C.c_longlong()
+        self._c("pic_get_particles_raw", s, C.byref(n), None, None, None, None, None, None)
+        m = n.value
+        a = dict(cell=np.empty(m, np.int32), ox=np.empty(m, np.float32),
+                 oy=np.empty(m, np.float32), vx=np.empty(m, np.float32),
+                 vy=np.empty(m, np.float32), pid=np.empty(m, np.uint32))
+        self._c("pic_get_particles_raw", s, C.byref(n), *[_ptr(a[k]) for k in
+                                                         ("cell", "ox", "oy", "vx", "vy", "pid")])
+        return a
+
+    def particles_device(self, s=0) -> ParticlesView:
+        v = ParticlesView()
+        self._c("pic_particles_device", s, C.byref(v))
+        return v
+
+    # ---- stages
+    def prime_leapfrog(self):
+        self._c("pic_prime_leapfrog")
+
+    def sort(self):
+        self._c("pic_sort")
+
+    def deposit(self):
+        self._c("pic_deposit")
+
+    def poisson(self):
+        self._c("pic_poisson")
+
+    def gather_push(self, deposit=True):
+        self._c("pic_gather_push", 1 if deposit else 0)
+
+    def collide(self, kind):
+        self._c("pic_collide", kind)
+
+    def step(self, n=1):
+        self._c("pic_step", int(n))
+
+    def synchronize(self):
+        self._c("pic_synchronize")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._c("pic_get_stream", C.byref(s))
+        return s.value or 0
+
+    def run_host(self, x, y, vx, vy, nsteps, prime=True, out=None):
+        n = len(x)
+        if out is None:
+            out = [np.empty(n) for _ in range(4)]
+        self._c("pic_run_host", n, _ptr(x), _ptr(y), _ptr(vx), _ptr(vy), int(nsteps),
+                1 if prime else 0, *[_ptr(o) for o in out])
+        return out
+
+    # ---- diagnostics
+    def diagnostics(self) -> Diag:
+        d = Diag()
+        self._c("pic_diagnostics", C.byref(d))
+        return d
+
+    def history(self, which, first, count):
+        out = np.empty(count)
+        self._c("pic_get_history", which, first, count, _ptr(out))
+        return out
+
+    def track_mode(self, mx, my):
+        self._c("pic_track_mode", mx, my)
+
+    def grid(self, which):
+        out = np.empty((self.cfg.ny, self.cfg.nx))
+        self._c("pic_get_grid", which, _ptr(out))
+        return out
+
+    def rho_fixed(self):
+        out = np.empty((self.cfg.ny, self.cfg.nx), np.int64)
+        self._c("pic_get_rho_fixed", _ptr(out))
+        return out

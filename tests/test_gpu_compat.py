@@ -1,0 +1,57 @@
+"""Reference-convention GPU path (pic_compat_run*, the picFloatGpu drop-in)
+against the reference's own CPU step: golden vectors made from the
+reference's sources, and the bit-exact C restatement for other inputs."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import picgpu as P
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+CASES = sorted(glob.glob(os.path.join(GOLDEN, "compat_*.npz")))
+INTS = {"xDim", "yDim", "nx", "ny", "npx", "npy"}
+
+
+def case(path):
+    z = np.load(path)
+    d = {str(k): (int(v) if str(k) in INTS else float(v)) for k, v in zip(z["param_keys"], z["params"])}
+    return P.ref_params(**d), z
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(c) for c in CASES])
+def test_compat_steps_match_reference(path):
+    p, z = case(path)
+    out = P.compat_run_steps(p, z["x0"], z["y0"], z["vx0"], z["vy0"], int(z["nsteps"]))
+    # FP64 throughout; the GPU sums the deposit with atomics and transforms with
+    # cuFFT, so agreement is to rounding, far inside the reference's own 1e-4
+    # position check (collisionless/double/src/main.cc:260)
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_allclose(out[k], z[k], rtol=0, atol=1e-9, err_msg=k)
+    for k in ("rho", "phi", "ex", "ey"):
+        scale = max(np.abs(z[k]).max(), 1e-300)
+        np.testing.assert_allclose(out[k], z[k], rtol=0, atol=1e-10 * scale, err_msg=k)
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(c) for c in CASES])
+def test_compat_run_counts_steps_like_reference(path):
+    p, z = case(path)
+    xo, yo, sec = P.compat_run(p, z["x0"], z["y0"], z["vx0"], z["vy0"])
+    ref = P.compat_run_steps(p, z["x0"], z["y0"], z["vx0"], z["vy0"], int(z["loop_steps"]))
+    np.testing.assert_array_equal(xo, ref["x"])
+    np.testing.assert_array_equal(yo, ref["y"])
+    assert sec > 0
+
+
+def test_compat_larger_case_vs_restatement():
+    p = O.ref_params(xDim=16, yDim=16, nx=64, ny=64, npx=200, npy=150, dt=0.005, tmax=1.0,
+                     charge=-20.0, mass=5.0, vtx=1.0, vty=1.0, vdx=0.5, vdy=0.0)
+    x, y, vx, vy = O.compat_init(p, seed=11)
+    ref = O.compat_run(p, x, y, vx, vy, 30, nthreads=0)
+    out = P.compat_run_steps(P.ref_params(**{f[0]: getattr(p, f[0]) for f in p._fields_}),
+                             x, y, vx, vy, 30)
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_allclose(out[k], ref[k], rtol=0, atol=1e-9, err_msg=k)

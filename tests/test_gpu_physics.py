@@ -1,0 +1,116 @@
+"""Physics-mode step against the FP64 oracle and conservation laws."""
+import numpy as np
+import pytest
+
+import oracle as O
+import picgpu as P
+from gpu_util import normalized_electrons, oracle_from_handle, periodic_diff
+
+pytestmark = pytest.mark.gpu
+
+
+def test_short_run_matches_fp64_oracle():
+    nx = ny = 64
+    L = 2 * np.pi * 2
+    n = nx * ny * 16
+    cfg, q, m = normalized_electrons(nx, ny, L, L, n, 0.1)
+    with P.Handle(cfg) as h:
+        h.init_particles(0, P.init_spec(n, vth=(0.05, 0.05, 0), pert_kind=P.PERT_DENSITY,
+                                        pert_amp=0.05, pert_mx=1, pert_my=1, seed=3))
+        st = oracle_from_handle(h, cfg, q, m)
+        f0 = st.fields(nthreads=0)
+        assert h.diagnostics().field_energy == pytest.approx(f0["fe"], rel=1e-4)
+        np.testing.assert_allclose(h.grid(P.GRID_EX), f0["ex"], atol=1e-4 * np.abs(f0["ex"]).max())
+        h.prime_leapfrog()
+        st.prime(nthreads=0)
+        nst = 40
+        h.step(nst)
+        ref = st.run(nst, nthreads=0)
+        fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
+        rel = np.abs(fe - ref["fe"]) / ref["fe"].max()
+        print("field energy max rel err", rel.max())
+        assert rel.max() < 2e-4
+        ke = h.history(P.HIST_KINETIC, 0, nst)
+        np.testing.assert_allclose(ke, ref["ke"], rtol=2e-4)
+        a = h.get_particles()
+        s = st.species[0]
+        dxp = periodic_diff(a["x"], s["x"], L)
+        dyp = periodic_diff(a["y"], s["y"], L)
+        print("position max abs err (cells)", np.abs(dxp).max() / (L / nx))
+        assert np.abs(dxp).max() < 1e-3 * L / nx
+        assert np.abs(dyp).max() < 1e-3 * L / ny
+        np.testing.assert_allclose(a["vx"], s["vx"], atol=1e-4 * np.abs(s["vx"]).max())
+
+
+def test_energy_conserved_and_charge_exact():
+    nx = ny = 32
+    L = 2 * np.pi
+    n = nx * ny * 64
+    cfg, q, m = normalized_electrons(nx, ny, L, L, n, 0.05)
+    with P.Handle(cfg) as h:
+        h.init_particles(0, P.init_spec(n, layout=P.LOAD_LATTICE, pert_kind=P.PERT_XDISP,
+                                        pert_amp=0.02, pert_mx=1, vth=(0.0, 0.0, 0), seed=1))
+        h.prime_leapfrog()
+        h.step(400)
+        h.synchronize()
+        fe = h.history(P.HIST_FIELD_ENERGY, 0, 400)
+        ke = h.history(P.HIST_KINETIC, 0, 400)
+        tot = fe + ke
+        print("energy drift", np.ptp(tot) / tot.max())
+        assert np.ptp(tot) < 5e-3 * tot.max()
+        assert (h.history(P.HIST_CHARGE, 0, 401) == -n * 2.0**32).all()
+        d = h.diagnostics()
+        assert d.error_flags == 0 and d.step == 400
+
+
+def run_state(cfg, n, nsteps, seed, eager=False):
+    with P.Handle(cfg) as h:
+        h.init_particles(0, P.init_spec(n, vth=(0.4, 0.4, 0), seed=seed))
+        h.prime_leapfrog()
+        if eager:
+            for _ in range(nsteps):
+                h.gather_push(True)
+                h.poisson()
+        else:
+            h.step(nsteps)
+        a = h.get_particles()
+        return a, h.rho_fixed(), h.history(P.HIST_FIELD_ENERGY, 0, nsteps + 1)
+
+
+def test_results_independent_of_sort_cadence_and_graphs():
+    nx, ny = 64, 32
+    n = nx * ny * 20
+    cfg1, _, _ = normalized_electrons(nx, ny, 8.0, 4.0, n, 0.1, sort_every=1)
+    cfg2, _, _ = normalized_electrons(nx, ny, 8.0, 4.0, n, 0.1, sort_every=7, chunk=512)
+    a1, r1, f1 = run_state(cfg1, n, 15, seed=4)
+    a2, r2, f2 = run_state(cfg2, n, 15, seed=4)
+    a3, r3, f3 = run_state(cfg2, n, 15, seed=4, eager=True)
+    for k in a1:
+        np.testing.assert_array_equal(a1[k], a2[k], err_msg=k)
+        np.testing.assert_array_equal(a2[k], a3[k], err_msg=k)
+    np.testing.assert_array_equal(r1, r2)
+    np.testing.assert_array_equal(r2, r3)
+    np.testing.assert_array_equal(f1, f2)
+
+
+def test_init_matches_restatement():
+    nx, ny, L = 32, 16, 5.0
+    n = nx * ny * 8
+    cfg, q, m = normalized_electrons(nx, ny, L, L / 2, n, 0.1)
+    spec = P.init_spec(n, vth=(0.1, 0.2, 0), vdrift=(0.01, 0.0), beam_v=0.3, seed=0x1234_5678_9)
+    with P.Handle(cfg) as h:
+        h.init_particles(0, spec)
+        a = h.get_particles()
+    i = np.arange(n)
+    k0, k1 = spec.seed & 0xFFFFFFFF, spec.seed >> 32
+    r0 = np.array([O.philox4x32_10([j & 0xFFFFFFFF, j >> 32, 0, 0x696E6974], [k0, k1]) for j in i])
+    r1 = np.array([O.philox4x32_10([j & 0xFFFFFFFF, j >> 32, 1, 0x696E6974], [k0, k1]) for j in i])
+    u = lambda r: (r.astype(np.float64) + 0.5) / 2**32
+    uf = lambda r: ((r >> 8).astype(np.float64) + 0.5) / 2**24
+    np.testing.assert_allclose(a["x"], u(r0[:, 0]) * L, atol=1e-6 * L)
+    np.testing.assert_allclose(a["y"], u(r0[:, 1]) * L / 2, atol=1e-6 * L)
+    rad = np.sqrt(-2 * np.log(uf(r0[:, 2])))
+    vx = 0.01 + 0.1 * rad * np.cos(2 * np.pi * uf(r0[:, 3])) + np.where(i & 1, -0.3, 0.3)
+    vy = 0.2 * rad * np.sin(2 * np.pi * uf(r0[:, 3]))
+    np.testing.assert_allclose(a["vx"], vx, atol=2e-6)
+    np.testing.assert_allclose(a["vy"], vy, atol=2e-6)
