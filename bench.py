@@ -187,6 +187,7 @@ def run_reference(args):
 
 
 def main():
+    global NX, NY, N, L, SORT_EVERY
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=60)
@@ -194,7 +195,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nx", type=int, default=NX, help="cells per side (profiling on smaller cases)")
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--tile", type=int, nargs=2, default=(0, 0))
+    ap.add_argument("--sort-every", type=int, default=SORT_EVERY)
     args = ap.parse_args()
+    NX = NY = args.nx
+    N = NX * NY * PPC
+    L = NX * DX
+    SORT_EVERY = args.sort_every
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -221,7 +230,8 @@ def main():
 
     A = L * L
     sp = P.species(N, -A / N, A / N, -1)
-    cfg = P.config(NX, NY, L, L, DT, [sp], sort_every=SORT_EVERY, device=local)
+    cfg = P.config(NX, NY, L, L, DT, [sp], sort_every=SORT_EVERY, device=local,
+                   chunk=args.chunk, tile_w=args.tile[0], tile_h=args.tile[1])
     h = P.Handle(cfg)
     spec = P.init_spec(N, vth=(VTH, VTH, 0), pert_kind=P.PERT_DENSITY, pert_amp=0.01,
                        pert_mx=1, pert_my=1, seed=2024 + rank)

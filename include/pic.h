@@ -119,7 +119,7 @@ typedef struct pic_config {
     pic_species_desc species[PIC_MAX_SPECIES];
     int sort_every;      /* steps between counting sorts (0: 20)              */
     int tile_w, tile_h;  /* sort tile in cells (0: chosen from the density)   */
-    int chunk;           /* particles per push block, multiple of 4 (0: auto) */
+    int chunk;           /* particles per push block, multiple of 4 (0: 8192) */
     int halo;            /* shared-memory window halo in cells (0: 2)         */
     int history;         /* diagnostic history length in steps (0: 4096)      */
     int device;          /* CUDA device ordinal                               */

@@ -43,7 +43,12 @@ convert_kernel(unsigned long long *__restrict__ rho_fix, float *__restrict__ rho
         const unsigned long long v = rho_fix[i];
         rho_fix[i] = 0ull;
         qs += v;
-        rho[i] = __ll2float_rn((long long)v - mean_fix) * scale;
+        // int64 -> float as hi * 2^32 + lo: two fast 32-bit conversions and
+        // one fma (at most one extra rounding) instead of the slow 64-bit
+        // conversion
+        const long long d = (long long)v - mean_fix;
+        const float f = fmaf((float)(int)(d >> 32), 4294967296.0f, (float)(unsigned)(d & 0xFFFFFFFFll));
+        rho[i] = f * scale;
     }
     qs = warp_sum_u64(qs);
     if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = qs;

@@ -160,7 +160,7 @@ static pic_status setup_geometry(pic_handle *h)
     g.Ly = c.Ly;
     g.dx = c.Lx / c.nx;
     g.dy = c.Ly / c.ny;
-    g.chunk = c.chunk ? c.chunk : 2048;
+    g.chunk = c.chunk ? c.chunk : 8192;
     g.halo = c.halo ? c.halo : 2;
     long long maxcap = 0;
     for (int s = 0; s < c.nspecies; ++s) maxcap = std::max(maxcap, c.species[s].capacity);

@@ -20,18 +20,20 @@ struct InitArgs {
     uint32_t *pid;
     long long n;
     int nx, ny;
-    double Lx, Ly, dx, dy;
+    double Lx, Ly, dx, dy, inv_dx, inv_dy;
     int layout, pert_kind, lat_nx, lat_ny;
     double vth0, vth1, vth2, vd0, vd1, beam_v, amp;
     double kx, ky;  // perturbation wavevector
     uint32_t k0, k1;
 };
 
-// global position -> (cell, offset) with periodic wrap
-__device__ __forceinline__ void locate(double x, double L, double d, int n, int &c, float &o)
+// global position -> (cell, offset) with periodic wrap; inv_d = 1/d.  FP64
+// work is kept to a few multiplies (no division), and the wrap is skipped for
+// positions already inside [0, L).
+__device__ __forceinline__ void locate(double x, double L, double inv_d, int n, int &c, float &o)
 {
-    x -= L * floor(x / L);
-    double g = x / d;
+    if (!(x >= 0.0 && x < L)) x -= L * floor(x * (1.0 / L));
+    double g = x * inv_d;
     double f = floor(g);
     int i = (int)f;
     float fr = (float)(g - f);
@@ -71,8 +73,8 @@ __global__ void __launch_bounds__(256) init_kernel(InitArgs A)
         }
         int cx, cy;
         float ox, oy;
-        locate(x, A.Lx, A.dx, A.nx, cx, ox);
-        locate(y, A.Ly, A.dy, A.ny, cy, oy);
+        locate(x, A.Lx, 1.0 / A.dx, A.nx, cx, ox);
+        locate(y, A.Ly, 1.0 / A.dy, A.ny, cy, oy);
         // Box-Muller normals
         const float ra = sqrtf(-2.f * logf(u01f(r0.z)));
         float sa, ca;
@@ -100,8 +102,8 @@ __global__ void from_global_kernel(InitArgs A, const double *x, const double *y,
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += stride) {
         int cx, cy;
         float ox, oy;
-        locate(x[i], A.Lx, A.dx, A.nx, cx, ox);
-        locate(y[i], A.Ly, A.dy, A.ny, cy, oy);
+        locate(x[i], A.Lx, A.inv_dx, A.nx, cx, ox);
+        locate(y[i], A.Ly, A.inv_dy, A.ny, cy, oy);
         A.cell[i] = cx | (cy << 16);
         A.ox[i] = ox;
         A.oy[i] = oy;
@@ -161,6 +163,8 @@ static InitArgs base_args(pic_handle *h, int s)
     A.Ly = g.Ly;
     A.dx = g.dx;
     A.dy = g.dy;
+    A.inv_dx = 1.0 / g.dx;
+    A.inv_dy = 1.0 / g.dy;
     return A;
 }
 

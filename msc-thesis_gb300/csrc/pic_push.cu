@@ -21,9 +21,14 @@
 // the four node weights (2^16-fx)(2^16-fy), fx(2^16-fy), (2^16-fx)fy, fx fy
 // are integers that sum to 2^32 for every particle, so the density in
 // 2^-32 charge units is an integer sum, independent of summation order, and
-// the total charge is exact.  Before touching memory, lanes of a warp that
-// deposit into the same cell are combined (match.any + redux.sync): the
-// four weights of a group follow from the group sums of fx, fy and fx*fy.
+// the total charge is exact.  Each thread owns four consecutive particles of
+// the sorted array (one 128-bit load per field); those that land in the same
+// cell are combined in registers (the four weights of a group follow from the
+// group's count and sums of fx, fy and fx*fy) before one set of atomics.  In
+// shared memory every node keeps two 32-bit accumulators, the low 16 bits and
+// the rest of its unsigned weight, so the hot atomics are native 32-bit adds;
+// the charge sign is applied once per node when the window is flushed with a
+// 64-bit atomic to the global density.
 #include <cuda_runtime.h>
 
 #include "pic_internal.cuh"
@@ -34,34 +39,16 @@ struct Cic4 {
     unsigned long long w00, w10, w01, w11;
 };
 
-// Warp-aggregated fixed-point CIC weights.  Every lane of the warp must call
-// this (valid = false on lanes without a particle).  Returns true on the one
-// lane per distinct key that holds the group's summed weights.
-__device__ __forceinline__ bool aggregate_cic(bool valid, int key, float ox, float oy, Cic4 &W)
+// Node weights of `cnt` particles in one cell from their sums of fx, fy, fx*fy.
+__device__ __forceinline__ Cic4 cic_weights(unsigned cnt, unsigned sfx, unsigned sfy,
+                                            unsigned long long sxy)
 {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int k = valid ? key : (-1 - lane);  // lanes without a particle stay alone
-    const unsigned grp = __match_any_sync(full, k);
-    unsigned fx = 0u, fy = 0u;
-    if (valid) {
-        fx = __float2uint_rn(ox * 65536.0f);
-        fy = __float2uint_rn(oy * 65536.0f);
-    }
-    const unsigned long long p = (unsigned long long)fx * fy;  // <= 2^32
-    const unsigned plo = (unsigned)(p & 0xFFFFull), phi = (unsigned)(p >> 16);
-    const unsigned sfx = __reduce_add_sync(grp, fx);
-    const unsigned sfy = __reduce_add_sync(grp, fy);
-    const unsigned slo = __reduce_add_sync(grp, plo);
-    const unsigned shi = __reduce_add_sync(grp, phi);
-    if (!valid || lane != __ffs(grp) - 1) return false;
-    const unsigned long long cnt = (unsigned long long)__popc(grp);
-    const unsigned long long s11 = ((unsigned long long)shi << 16) + slo;
-    W.w11 = s11;
-    W.w10 = ((unsigned long long)sfx << 16) - s11;
-    W.w01 = ((unsigned long long)sfy << 16) - s11;
-    W.w00 = (cnt << 32) - (((unsigned long long)sfx + sfy) << 16) + s11;
-    return true;
+    Cic4 W;
+    W.w11 = sxy;
+    W.w10 = ((unsigned long long)sfx << 16) - sxy;
+    W.w01 = ((unsigned long long)sfy << 16) - sxy;
+    W.w00 = ((unsigned long long)cnt << 32) - ((unsigned long long)(sfx + sfy) << 16) + sxy;
+    return W;
 }
 
 __device__ __forceinline__ void deposit_global(unsigned long long *rho, int nx, int ny, int cx,
@@ -73,6 +60,12 @@ __device__ __forceinline__ void deposit_global(unsigned long long *rho, int nx, 
     atomicAdd(rho + (size_t)cy * nx + cx1, W.w10 * q);
     atomicAdd(rho + (size_t)cy1 * nx + cx, W.w01 * q);
     atomicAdd(rho + (size_t)cy1 * nx + cx1, W.w11 * q);
+}
+
+__device__ __forceinline__ void smem_add(unsigned *lo, unsigned *hi, int i, unsigned long long w)
+{
+    atomicAdd(lo + i, (unsigned)(w & 0xFFFFull));
+    atomicAdd(hi + i, (unsigned)(w >> 16));
 }
 
 struct PushArgs {
@@ -108,7 +101,8 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
 
     const int nwx = A.wcx + 1, nwy = A.wcy + 1, nw = nwx * nwy;
     float2 *sE = reinterpret_cast<float2 *>(smem);
-    unsigned long long *sR = reinterpret_cast<unsigned long long *>(smem + (size_t)nw * sizeof(float2));
+    unsigned *sLo = reinterpret_cast<unsigned *>(smem + (size_t)nw * sizeof(float2));
+    unsigned *sHi = sLo + nw;
     double *sAcc = reinterpret_cast<double *>(smem + (size_t)nw * 16);
 
     const int anc = A.anchor[blockIdx.x];
@@ -125,134 +119,141 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
             const int a = i % nwx, b = i / nwx;
             const int gx = (wx0 + a) % nx, gy = (wy0 + b) % ny;
             if (GATHER) sE[i] = make_float2(A.ex[(size_t)gy * nx + gx], A.ey[(size_t)gy * nx + gx]);
-            if (DEPOSIT) sR[i] = 0ull;
+            if (DEPOSIT) {
+                sLo[i] = 0u;
+                sHi[i] = 0u;
+            }
         }
     }
     if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
     __syncthreads();
 
+    // deposit of one group of particles in one cell: window or global
+    auto deposit = [&](int cx, int cy, const Cic4 &W) {
+        int dxl = cx - wx0, dyl = cy - wy0;
+        if (dxl < 0) dxl += nx;
+        if (dyl < 0) dyl += ny;
+        if (win && dxl < A.wcx && dyl < A.wcy) {
+            const int i = dyl * nwx + dxl;
+            smem_add(sLo, sHi, i, W.w00);
+            smem_add(sLo, sHi, i + 1, W.w10);
+            smem_add(sLo, sHi, i + nwx, W.w01);
+            smem_add(sLo, sHi, i + nwx + 1, W.w11);
+        } else {
+            deposit_global(A.rho, nx, ny, cx, cy, W, A.qmul);
+        }
+    };
+
     float ke = 0.f, px = 0.f, py = 0.f;
     bool bad = false;
-    for (long long q0 = base; q0 < end; q0 += 4ll * blockDim.x) {  // block-uniform trip count
-        const long long q = q0 + 4ll * threadIdx.x;
-        const bool live = q < end;
-        int cc[4] = {-1, -1, -1, -1};
-        float xo[4], yo[4], xv[4], yv[4];
-        if (live) {
-            const int4 c4 = __ldg(reinterpret_cast<const int4 *>(A.cin + q));
-            const float4 a4 = __ldg(reinterpret_cast<const float4 *>(A.oxin + q));
-            const float4 b4 = __ldg(reinterpret_cast<const float4 *>(A.oyin + q));
-            const float4 u4 = __ldg(reinterpret_cast<const float4 *>(A.vxin + q));
-            const float4 v4 = __ldg(reinterpret_cast<const float4 *>(A.vyin + q));
-            cc[0] = c4.x; cc[1] = c4.y; cc[2] = c4.z; cc[3] = c4.w;
-            xo[0] = a4.x; xo[1] = a4.y; xo[2] = a4.z; xo[3] = a4.w;
-            yo[0] = b4.x; yo[1] = b4.y; yo[2] = b4.z; yo[3] = b4.w;
-            xv[0] = u4.x; xv[1] = u4.y; xv[2] = u4.z; xv[3] = u4.w;
-            yv[0] = v4.x; yv[1] = v4.y; yv[2] = v4.z; yv[3] = v4.w;
-        } else {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) xo[j] = yo[j] = xv[j] = yv[j] = 0.f;
-        }
+    for (long long q = base + 4ll * threadIdx.x; q < end; q += 4ll * blockDim.x) {
+        // plain (coherent) loads: with an in-place pass the same addresses are stored below
+        const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
+        const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
+        const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
+        const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+        const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+        int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+        float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
+        float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
+        // register aggregate of the particles that share the first one's new cell
+        unsigned gcnt = 0u, gfx = 0u, gfy = 0u;
+        unsigned long long gxy = 0ull;
+        int gkey = -1, gcx = 0, gcy = 0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            int c = cc[j];
+            const int c = cc[j];
+            if (c < 0) continue;  // empty slot
             int cx = c & 0xFFFF, cy = c >> 16;
-            bool valid = c >= 0;
-            if (valid && (cx >= nx || cy >= ny)) {  // corrupt cell: flag, leave untouched
-                valid = false;
+            if (cx >= nx || cy >= ny) {  // corrupt cell: flag, leave untouched
                 bad = true;
                 atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_CELL);
+                continue;
             }
             float ox = xo[j], oy = yo[j], vx = xv[j], vy = yv[j];
-            if (valid) {
-                if (GATHER) {
-                    const float gx = 1.f - ox, gy = 1.f - oy;
-                    float2 e00, e10, e01, e11;
-                    int dxl = cx - wx0, dyl = cy - wy0;
-                    if (dxl < 0) dxl += nx;
-                    if (dyl < 0) dyl += ny;
-                    if (win && dxl < A.wcx && dyl < A.wcy) {
-                        const int i = dyl * nwx + dxl;
-                        e00 = sE[i];
-                        e10 = sE[i + 1];
-                        e01 = sE[i + nwx];
-                        e11 = sE[i + nwx + 1];
-                    } else {
-                        const int cx1 = (cx + 1 == nx) ? 0 : cx + 1;
-                        const int cy1 = (cy + 1 == ny) ? 0 : cy + 1;
-                        const size_t i00 = (size_t)cy * nx + cx, i10 = (size_t)cy * nx + cx1;
-                        const size_t i01 = (size_t)cy1 * nx + cx, i11 = (size_t)cy1 * nx + cx1;
-                        e00 = make_float2(A.ex[i00], A.ey[i00]);
-                        e10 = make_float2(A.ex[i10], A.ey[i10]);
-                        e01 = make_float2(A.ex[i01], A.ey[i01]);
-                        e11 = make_float2(A.ex[i11], A.ey[i11]);
-                    }
-                    const float Ex = gy * (gx * e00.x + ox * e10.x) + oy * (gx * e01.x + ox * e11.x);
-                    const float Ey = gy * (gx * e00.y + ox * e10.y) + oy * (gx * e01.y + ox * e11.y);
-                    const float vx0 = vx, vy0 = vy;
-                    vx = fmaf(A.qm_dt, Ex, vx);
-                    vy = fmaf(A.qm_dt, Ey, vy);
-                    ke += vx0 * vx0 + vy0 * vy0 + vx * vx + vy * vy;
-                    px += vx0 + vx;
-                    py += vy0 + vy;
+            if (GATHER) {
+                const float gx = 1.f - ox, gy = 1.f - oy;
+                float2 e00, e10, e01, e11;
+                int dxl = cx - wx0, dyl = cy - wy0;
+                if (dxl < 0) dxl += nx;
+                if (dyl < 0) dyl += ny;
+                if (win && dxl < A.wcx && dyl < A.wcy) {
+                    const int i = dyl * nwx + dxl;
+                    e00 = sE[i];
+                    e10 = sE[i + 1];
+                    e01 = sE[i + nwx];
+                    e11 = sE[i + nwx + 1];
                 } else {
-                    ke += 2.f * (vx * vx + vy * vy);
-                    px += 2.f * vx;
-                    py += 2.f * vy;
+                    const int cx1 = (cx + 1 == nx) ? 0 : cx + 1;
+                    const int cy1 = (cy + 1 == ny) ? 0 : cy + 1;
+                    const size_t i00 = (size_t)cy * nx + cx, i10 = (size_t)cy * nx + cx1;
+                    const size_t i01 = (size_t)cy1 * nx + cx, i11 = (size_t)cy1 * nx + cx1;
+                    e00 = make_float2(A.ex[i00], A.ey[i00]);
+                    e10 = make_float2(A.ex[i10], A.ey[i10]);
+                    e01 = make_float2(A.ex[i01], A.ey[i01]);
+                    e11 = make_float2(A.ex[i11], A.ey[i11]);
                 }
-                if (!isfinite(vx) || !isfinite(vy)) bad = true;
-                // drift in cell units; carry whole cells into the index
-                ox = fmaf(vx, A.dtdx, ox);
-                oy = fmaf(vy, A.dtdy, oy);
-                float sx = floorf(ox), sy = floorf(oy);
-                ox -= sx;
-                oy -= sy;
-                if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
-                if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
-                cx += (int)sx;
-                cy += (int)sy;
-                if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
-                if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
-                c = cx | (cy << 16);
+                const float Ex = gy * fmaf(gx, e00.x, ox * e10.x) + oy * fmaf(gx, e01.x, ox * e11.x);
+                const float Ey = gy * fmaf(gx, e00.y, ox * e10.y) + oy * fmaf(gx, e01.y, ox * e11.y);
+                const float vx0 = vx, vy0 = vy;
+                vx = fmaf(A.qm_dt, Ex, vx);
+                vy = fmaf(A.qm_dt, Ey, vy);
+                ke = fmaf(vx0, vx0, fmaf(vy0, vy0, fmaf(vx, vx, fmaf(vy, vy, ke))));
+                px += vx0 + vx;
+                py += vy0 + vy;
+            } else {
+                ke = fmaf(2.f * vx, vx, fmaf(2.f * vy, vy, ke));
+                px = fmaf(2.f, vx, px);
+                py = fmaf(2.f, vy, py);
             }
+            bad |= !(fabsf(vx) <= 3.0e38f) || !(fabsf(vy) <= 3.0e38f);
+            // drift in cell units; carry whole cells into the index
+            ox = fmaf(vx, A.dtdx, ox);
+            oy = fmaf(vy, A.dtdy, oy);
+            float sx = floorf(ox), sy = floorf(oy);
+            ox -= sx;
+            oy -= sy;
+            if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
+            if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
+            cx += (int)sx;
+            cy += (int)sy;
+            if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
+            if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
+            const int cn = cx | (cy << 16);
+            cc[j] = cn;
+            xo[j] = ox;
+            yo[j] = oy;
+            xv[j] = vx;
+            yv[j] = vy;
             if (DEPOSIT) {
-                Cic4 W;
-                if (aggregate_cic(valid, c, ox, oy, W)) {
-                    int dxl = cx - wx0, dyl = cy - wy0;
-                    if (dxl < 0) dxl += nx;
-                    if (dyl < 0) dyl += ny;
-                    if (win && dxl < A.wcx && dyl < A.wcy) {
-                        const int i = dyl * nwx + dxl;
-                        atomicAdd(sR + i, W.w00 * A.qmul);
-                        atomicAdd(sR + i + 1, W.w10 * A.qmul);
-                        atomicAdd(sR + i + nwx, W.w01 * A.qmul);
-                        atomicAdd(sR + i + nwx + 1, W.w11 * A.qmul);
-                    } else {
-                        deposit_global(A.rho, nx, ny, cx, cy, W, A.qmul);
-                    }
+                const unsigned fx = __float2uint_rn(ox * 65536.0f);
+                const unsigned fy = __float2uint_rn(oy * 65536.0f);
+                const unsigned long long fxy = (unsigned long long)fx * fy;
+                if (gkey < 0) {
+                    gkey = cn;
+                    gcx = cx;
+                    gcy = cy;
+                }
+                if (cn == gkey) {
+                    ++gcnt;
+                    gfx += fx;
+                    gfy += fy;
+                    gxy += fxy;
+                } else {
+                    deposit(cx, cy, cic_weights(1u, fx, fy, fxy));
                 }
             }
-            if (valid) {
-                cc[j] = c;
-                xo[j] = ox;
-                yo[j] = oy;
-                xv[j] = vx;
-                yv[j] = vy;
-            }
         }
-        if (live) {
-            *reinterpret_cast<int4 *>(A.cout + q) = make_int4(cc[0], cc[1], cc[2], cc[3]);
-            *reinterpret_cast<float4 *>(A.oxout + q) = make_float4(xo[0], xo[1], xo[2], xo[3]);
-            *reinterpret_cast<float4 *>(A.oyout + q) = make_float4(yo[0], yo[1], yo[2], yo[3]);
-            *reinterpret_cast<float4 *>(A.vxout + q) = make_float4(xv[0], xv[1], xv[2], xv[3]);
-            *reinterpret_cast<float4 *>(A.vyout + q) = make_float4(yv[0], yv[1], yv[2], yv[3]);
-            if (A.pidin)
-                *reinterpret_cast<uint4 *>(A.pidout + q) =
-                    __ldg(reinterpret_cast<const uint4 *>(A.pidin + q));
-            if (A.vzin)
-                *reinterpret_cast<float4 *>(A.vzout + q) =
-                    __ldg(reinterpret_cast<const float4 *>(A.vzin + q));
-        }
+        if (DEPOSIT && gcnt) deposit(gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+        *reinterpret_cast<int4 *>(A.cout + q) = make_int4(cc[0], cc[1], cc[2], cc[3]);
+        *reinterpret_cast<float4 *>(A.oxout + q) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+        *reinterpret_cast<float4 *>(A.oyout + q) = make_float4(yo[0], yo[1], yo[2], yo[3]);
+        *reinterpret_cast<float4 *>(A.vxout + q) = make_float4(xv[0], xv[1], xv[2], xv[3]);
+        *reinterpret_cast<float4 *>(A.vyout + q) = make_float4(yv[0], yv[1], yv[2], yv[3]);
+        if (A.pidin)
+            *reinterpret_cast<uint4 *>(A.pidout + q) = *reinterpret_cast<const uint4 *>(A.pidin + q);
+        if (A.vzin)
+            *reinterpret_cast<float4 *>(A.vzout + q) = *reinterpret_cast<const float4 *>(A.vzin + q);
     }
 
     // diagnostics: FP32 per thread and per warp, FP64 across warps and blocks
@@ -280,18 +281,18 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
     }
     if (DEPOSIT && win) {
         for (int i = threadIdx.x; i < nw; i += blockDim.x) {
-            const unsigned long long v = sR[i];
+            const unsigned long long v = ((unsigned long long)sHi[i] << 16) + sLo[i];
             if (v) {
                 const int a = i % nwx, b = i / nwx;
                 const int gx = (wx0 + a) % nx, gy = (wy0 + b) % ny;
-                atomicAdd(A.rho + (size_t)gy * nx + gx, v);
+                atomicAdd(A.rho + (size_t)gy * nx + gx, v * A.qmul);
             }
         }
     }
 }
 
-// Deposit-only pass (used after a sort/import, before the first step):
-// warp-aggregated fixed-point CIC straight to the global density.
+// Deposit-only pass (after a sort or an import, before the first step):
+// fixed-point CIC straight to the global density, one particle per thread.
 __global__ void __launch_bounds__(256)
 deposit_flat_kernel(const int32_t *__restrict__ cell, const float *__restrict__ ox,
                     const float *__restrict__ oy, const long long *d_n, long long n_host,
@@ -300,23 +301,18 @@ deposit_flat_kernel(const int32_t *__restrict__ cell, const float *__restrict__ 
 {
     const long long n = d_n ? *d_n : n_host;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long b = (long long)blockIdx.x * blockDim.x; b < n; b += stride) {  // warp-uniform
-        const long long i = b + threadIdx.x;
-        int c = -1;
-        float x = 0.f, y = 0.f;
-        if (i < n) {
-            c = cell[i];
-            x = ox[i];
-            y = oy[i];
-        }
-        int cx = c & 0xFFFF, cy = c >> 16;
-        bool valid = c >= 0;
-        if (valid && (cx >= nx || cy >= ny)) {
-            valid = false;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int c = cell[i];
+        if (c < 0) continue;
+        const int cx = c & 0xFFFF, cy = c >> 16;
+        if (cx >= nx || cy >= ny) {
             if (err) atomicOr(err, (unsigned)PIC_DEVERR_CELL);
+            continue;
         }
-        Cic4 W;
-        if (aggregate_cic(valid, c, x, y, W)) deposit_global(rho, nx, ny, cx, cy, W, qmul);
+        const unsigned fx = __float2uint_rn(ox[i] * 65536.0f);
+        const unsigned fy = __float2uint_rn(oy[i] * 65536.0f);
+        deposit_global(rho, nx, ny, cx, cy, cic_weights(1u, fx, fy, (unsigned long long)fx * fy),
+                       qmul);
     }
 }
 

@@ -6,9 +6,15 @@
 // the GPU) with a stable-layout counting sort:
 //   key(cell) = ((ty * ntx + tx) * th + ly) * tw + lx  for the tile (tx, ty)
 //               and the in-tile coordinates (lx, ly);
-//   1. histogram of keys            (warp-aggregated atomics)
+//   1. histogram of keys            (block-local shared-memory counts)
 //   2. exclusive scan -> offsets    (three-kernel block scan)
-//   3. scatter buffer 0 -> buffer 1 (warp-aggregated cursor atomics)
+//   3. scatter buffer 0 -> buffer 1 (block-local ranks, one global cursor
+//                                    atomic per distinct key and block)
+// The arrays are already nearly sorted from the previous sort, so the keys of
+// a block's SORT_CHUNK consecutive particles fall in a short range: a block
+// counts and ranks keys within a window of SORT_KEYS keys around its middle
+// particle's key in shared memory and touches global memory once per
+// distinct key; keys outside the window use global atomics directly.
 // After the scatter, offset[key] .. offset[key+1] is the slice of cell `key`
 // and every push chunk knows the tile of its first particle (anchor).
 #include <cuda_runtime.h>
@@ -39,24 +45,60 @@ struct SortArgs {
     unsigned int *err;
 };
 
-__global__ void __launch_bounds__(256) sort_hist_kernel(SortArgs A)
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_PER_THREAD = 16;
+constexpr int SORT_CHUNK = SORT_THREADS * SORT_PER_THREAD;
+constexpr int SORT_KEYS = 2048;
+
+// key of particle i, or -1 for an empty slot or a corrupt cell (flagged)
+__device__ __forceinline__ int particle_key(const SortArgs &A, long long i)
 {
+    const int c = A.cin[i];
+    if (c < 0) return -1;
+    const int cx = c & 0xFFFF, cy = c >> 16;
+    if (cx >= A.nx || cy >= A.ny) {
+        atomicOr(A.err, (unsigned)PIC_DEVERR_CELL);
+        return -1;
+    }
+    return cell_key(c, A.tw, A.th, A.ntx);
+}
+
+// first key of this block's shared-memory window (block-uniform)
+__device__ __forceinline__ int window_start(const SortArgs &A, long long base, long long n)
+{
+    const long long mid = min(base + SORT_CHUNK / 2, n - 1);
+    const int c = A.cin[mid];
+    int k = 0;
+    if (c >= 0 && (c & 0xFFFF) < A.nx && (c >> 16) < A.ny) k = cell_key(c, A.tw, A.th, A.ntx);
+    return max(0, k - SORT_KEYS / 2);
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
+{
+    __shared__ uint32_t s_cnt[SORT_KEYS];
     const long long n = *A.d_n;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31;
-    for (long long b = (long long)blockIdx.x * blockDim.x; b < n; b += stride) {  // warp-uniform
-        const long long i = b + threadIdx.x;
-        int key = -1 - lane;
-        if (i < n) {
-            const int c = A.cin[i];
-            const int cx = c & 0xFFFF, cy = c >> 16;
-            if (c >= 0 && cx < A.nx && cy < A.ny)
-                key = cell_key(c, A.tw, A.th, A.ntx);
-            else
-                atomicOr(A.err, (unsigned)PIC_DEVERR_CELL);
-        }
-        const unsigned grp = __match_any_sync(0xffffffffu, key);
-        if (key >= 0 && lane == __ffs(grp) - 1) atomicAdd(A.count + key, (uint32_t)__popc(grp));
+    const long long base = (long long)blockIdx.x * SORT_CHUNK;
+    if (base >= n) return;
+    const long long ncell = (long long)A.nx * A.ny;
+    const int k0 = window_start(A, base, n);
+    for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) s_cnt[r] = 0u;
+    __syncthreads();
+#pragma unroll 4
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
+        if (i >= n) break;
+        const int key = particle_key(A, i);
+        if (key < 0) continue;
+        const unsigned r = (unsigned)(key - k0);
+        if (r < (unsigned)SORT_KEYS)
+            atomicAdd(s_cnt + r, 1u);
+        else
+            atomicAdd(A.count + key, 1u);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) {
+        const uint32_t v = s_cnt[r];
+        if (v && k0 + r < ncell) atomicAdd(A.count + k0 + r, v);
     }
 }
 
@@ -149,40 +191,72 @@ scan_add_kernel(uint32_t *__restrict__ off, uint32_t *__restrict__ cursor, long 
     if (blockIdx.x == 0 && threadIdx.x == 0) off[n] = (uint32_t)*d_total;
 }
 
-__global__ void __launch_bounds__(256) sort_scatter_kernel(SortArgs A)
+__device__ __forceinline__ void move_particle(const SortArgs &A, long long i, long long d)
+{
+    A.cout[d] = A.cin[i];
+    A.oxout[d] = A.oxin[i];
+    A.oyout[d] = A.oyin[i];
+    A.vxout[d] = A.vxin[i];
+    A.vyout[d] = A.vyin[i];
+    A.pidout[d] = A.pidin[i];
+    if (A.vzin) A.vzout[d] = A.vzin[i];
+}
+
+// Tile of the first particle of every push chunk, read from the sorted array.
+__global__ void sort_anchor_kernel(SortArgs A, long long nchunks)
 {
     const long long n = *A.d_n;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31;
-    const int tcells = A.tw * A.th;
-    for (long long b = (long long)blockIdx.x * blockDim.x; b < n; b += stride) {  // warp-uniform
-        const long long i = b + threadIdx.x;
-        int key = -1 - lane, c = -1;
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nchunks || b * A.chunk >= n) return;
+    const int c = A.cout[b * A.chunk];
+    if (c < 0 || (c & 0xFFFF) >= A.nx || (c >> 16) >= A.ny) return;
+    const int t = cell_key(c, A.tw, A.th, A.ntx) / (A.tw * A.th);
+    A.anchor[b] = (t % A.ntx) | ((t / A.ntx) << 16);
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) sort_scatter_kernel(SortArgs A)
+{
+    __shared__ uint32_t s_cnt[SORT_KEYS];
+    __shared__ uint32_t s_base[SORT_KEYS];
+    const long long n = *A.d_n;
+    const long long base = (long long)blockIdx.x * SORT_CHUNK;
+    if (base >= n) return;
+    const long long ncell = (long long)A.nx * A.ny;
+    const int k0 = window_start(A, base, n);
+    for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) s_cnt[r] = 0u;
+    __syncthreads();
+    int keys[SORT_PER_THREAD];
+#pragma unroll
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
+        keys[j] = -1;
         if (i < n) {
-            c = A.cin[i];
-            const int cx = c & 0xFFFF, cy = c >> 16;
-            if (c >= 0 && cx < A.nx && cy < A.ny) key = cell_key(c, A.tw, A.th, A.ntx);
+            const int c = A.cin[i];
+            if (c >= 0 && (c & 0xFFFF) < A.nx && (c >> 16) < A.ny) keys[j] = cell_key(c, A.tw, A.th, A.ntx);
         }
-        const unsigned grp = __match_any_sync(0xffffffffu, key);
-        const int leader = __ffs(grp) - 1;
-        uint32_t base = 0;
-        if (key >= 0 && lane == leader) base = atomicAdd(A.cursor + key, (uint32_t)__popc(grp));
-        base = __shfl_sync(grp, base, leader);
+        const unsigned r = (unsigned)(keys[j] - k0);
+        if (keys[j] >= 0 && r < (unsigned)SORT_KEYS) atomicAdd(s_cnt + r, 1u);
+    }
+    __syncthreads();
+    // reserve each distinct key's slice of the output once per block
+    for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) {
+        const uint32_t v = s_cnt[r];
+        s_base[r] = (v && k0 + r < ncell) ? atomicAdd(A.cursor + k0 + r, v) : 0u;
+        s_cnt[r] = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        const int key = keys[j];
         if (key < 0) continue;
-        const uint32_t rank = __popc(grp & ((1u << lane) - 1u));
-        const long long d = (long long)base + rank;
-        A.cout[d] = c;
-        A.oxout[d] = A.oxin[i];
-        A.oyout[d] = A.oyin[i];
-        A.vxout[d] = A.vxin[i];
-        A.vyout[d] = A.vyin[i];
-        A.pidout[d] = A.pidin[i];
-        if (A.vzin) A.vzout[d] = A.vzin[i];
-        if (d % A.chunk == 0) {
-            const int t = key / tcells;
-            const int ntx = A.ntx;
-            A.anchor[d / A.chunk] = (t % ntx) | ((t / ntx) << 16);
-        }
+        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
+        const unsigned r = (unsigned)(key - k0);
+        long long d;
+        if (r < (unsigned)SORT_KEYS)
+            d = (long long)s_base[r] + atomicAdd(s_cnt + r, 1u);
+        else
+            d = atomicAdd(A.cursor + key, 1u);
+        move_particle(A, i, d);
     }
 }
 
@@ -221,8 +295,8 @@ pic_status launch_sort(pic_handle *h, int s)
     A.err = &h->dev->err;
     PIC_CUDA(cudaMemsetAsync(h->count, 0, sizeof(uint32_t) * (size_t)ncell, h->stream));
     PIC_CUDA(cudaMemsetAsync(B.anchor, 0xFF, sizeof(int32_t) * (size_t)B.nchunks, h->stream));
-    const int gp = grid_for(B.cap, 256);
-    sort_hist_kernel<<<gp, 256, 0, h->stream>>>(A);
+    const unsigned gp = (unsigned)((B.cap + SORT_CHUNK - 1) / SORT_CHUNK);
+    sort_hist_kernel<<<gp, SORT_THREADS, 0, h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     scan_blocks_kernel<<<h->scan_blocks, 1024, 0, h->stream>>>(h->count, h->offset, ncell, h->bsum);
     PIC_CUDA(cudaGetLastError());
@@ -231,7 +305,9 @@ pic_status launch_sort(pic_handle *h, int s)
     scan_add_kernel<<<grid_for(ncell, 256), 256, 0, h->stream>>>(h->offset, h->cursor, ncell,
                                                                h->bsum, &h->dev->n[s]);
     PIC_CUDA(cudaGetLastError());
-    sort_scatter_kernel<<<gp, 256, 0, h->stream>>>(A);
+    sort_scatter_kernel<<<gp, SORT_THREADS, 0, h->stream>>>(A);
+    PIC_CUDA(cudaGetLastError());
+    sort_anchor_kernel<<<(unsigned)((B.nchunks + 255) / 256), 256, 0, h->stream>>>(A, B.nchunks);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }
