@@ -264,6 +264,22 @@ pic_status pic_deposit_grid(int nx, int ny, long long n, const int32_t *cell_dev
                             const float *ox_dev, const float *oy_dev, int q_int, double scale,
                             double *rho_dev, void *stream);
 
+/* The same deposit without any device allocation, for callers that cannot
+ * call cudaMalloc: a framework that owns the GPU's memory through its own
+ * pool, a process held to a fixed device-memory budget, or a loop that must
+ * not pay cudaFree's device-wide synchronisation.  No counterpart in the
+ * reference.  The int64 scratch grid is a static device array of
+ * PIC_NOALLOC_MAX_CELLS cells (8 MiB held on every GPU that loads the
+ * library); nx*ny above that is rejected with PIC_ERR_INVALID_ARG.  The call
+ * only enqueues work on `stream` (NULL: legacy default stream) and returns.
+ * All calls share the scratch grid: calls whose work overlaps on the GPU
+ * race.  The first call on a device looks up the scratch address with that
+ * device current; make it before any stream capture on that device. */
+#define PIC_NOALLOC_MAX_CELLS (1 << 20)
+pic_status pic_deposit_grid_noalloc(int nx, int ny, long long n, const int32_t *cell_dev,
+                                    const float *ox_dev, const float *oy_dev, int q_int,
+                                    double scale, double *rho_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -121,7 +121,10 @@ SIGNATURES = {
     "pic_get_rho_fixed": [_H, _vp],
     "pic_deposit_grid": [C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp, C.c_int, C.c_double,
                          _vp, _vp],
+    "pic_deposit_grid_noalloc": [C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp, C.c_int,
+                                 C.c_double, _vp, _vp],
 }
+NOALLOC_MAX_CELLS = 1 << 20
 _RESTYPES = {"pic_status_string": C.c_char_p, "pic_last_error": C.c_char_p,
              "pic_version": C.c_char_p}
 
@@ -196,6 +199,14 @@ def deposit_grid(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale, rho_ptr, str
     """Stateless deposit of device arrays (integer device pointers)."""
     _check(load().pic_deposit_grid(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale, rho_ptr,
                                    stream), "pic_deposit_grid")
+
+
+def deposit_grid_noalloc(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale, rho_ptr,
+                         stream=None):
+    """The same deposit from the library's static scratch grid: allocates no
+    device memory; enqueues on `stream` and returns (see include/pic.h)."""
+    _check(load().pic_deposit_grid_noalloc(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale,
+                                           rho_ptr, stream), "pic_deposit_grid_noalloc")
 
 
 # ------------------------------------------------------------ handle ----
