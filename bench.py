@@ -45,6 +45,11 @@ SORT_EVERY = 20
 # write+read 16, R2C 8, k-space 12, 2 x C2R 16, field window read 8)
 BYTES_PER_PARTICLE = 40
 BYTES_PER_CELL = 60
+# DRAM bytes per particle of one push_kernel launch, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum = 688.1 + 618.3 MB for
+# 33,554,432 particles at 1024^2, profiles/push_kernel_landau-1024x1024-32ppc.md);
+# the kernel's traffic grows in proportion to the particles it processes
+TRAFFIC_PER_PARTICLE = (688.1e6 + 618.3e6) / 33554432
 
 
 def peaks():
@@ -328,7 +333,7 @@ def main():
                        "charge_exact": diag.total_charge_fixed == diag.expected_charge_fixed,
                        "field_energy": diag.field_energy},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
+                         "frac": achieved / hbm, "traffic": TRAFFIC_PER_PARTICLE * N,
                          "kernel": "push_kernel (fused gather+push+deposit)",
                          "kernel_ms": push_ms},
             "cpu_baseline": cpu,
