@@ -136,7 +136,12 @@ pic_status pic_get_stream(pic_handle *h, void **stream);
 pic_status pic_synchronize(pic_handle *h);
 
 enum pic_load { PIC_LOAD_RANDOM = 0, PIC_LOAD_LATTICE = 1 };
-enum pic_pert { PIC_PERT_NONE = 0, PIC_PERT_XDISP = 1, PIC_PERT_DENSITY = 2 };
+enum pic_pert {
+    PIC_PERT_NONE = 0,
+    PIC_PERT_XDISP = 1,   /* x += amp cos(kx x)                                  */
+    PIC_PERT_DENSITY = 2, /* n ~ 1 + amp cos(k.x), by displacement along k        */
+    PIC_PERT_BEAM_MODE = 3 /* per beam b: x += Re(xi_b e^{i kx x}), vx += Re(u_b e^{i kx x}) */
+};
 
 typedef struct pic_init_spec {
     long long n;        /* particles to create                                */
@@ -148,6 +153,10 @@ typedef struct pic_init_spec {
     double pert_amp;    /* XDISP: x += amp cos(kx x); DENSITY: n ~ 1+amp cos(k.x) */
     int pert_mx, pert_my; /* perturbation mode numbers (k = 2 pi m / L)       */
     unsigned long long seed;
+    /* PIC_PERT_BEAM_MODE: complex amplitudes (re, im) per beam, beam 0 = even
+     * ids (+beam_v), beam 1 = odd ids; lets a caller load a linear eigenmode */
+    double beam_xi[2][2];
+    double beam_u[2][2];
 } pic_init_spec;
 
 /* Create spec->n particles of a species on the device (Philox streams keyed

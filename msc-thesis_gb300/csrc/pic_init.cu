@@ -24,6 +24,7 @@ struct InitArgs {
     int layout, pert_kind, lat_nx, lat_ny;
     double vth0, vth1, vth2, vd0, vd1, beam_v, amp;
     double kx, ky;  // perturbation wavevector
+    double xi[2][2], uu[2][2];  // PIC_PERT_BEAM_MODE amplitudes per beam (re, im)
     uint32_t k0, k1;
 };
 
@@ -62,8 +63,15 @@ __global__ void __launch_bounds__(256) init_kernel(InitArgs A)
             x = u01d(r0.x) * A.Lx;
             y = u01d(r0.y) * A.Ly;
         }
+        double dvx = 0.0;
         if (A.pert_kind == PIC_PERT_XDISP) {
             x += A.amp * cos(A.kx * x);
+        } else if (A.pert_kind == PIC_PERT_BEAM_MODE) {
+            const int b = (int)(i & 1);
+            double sk, ck;
+            sincos(A.kx * x, &sk, &ck);
+            dvx = A.uu[b][0] * ck - A.uu[b][1] * sk;
+            x += A.xi[b][0] * ck - A.xi[b][1] * sk;
         } else if (A.pert_kind == PIC_PERT_DENSITY) {
             // displacement -(amp/|k|^2) k sin(k.x) gives n ~ 1 + amp cos(k.x) to first order
             const double k2 = A.kx * A.kx + A.ky * A.ky;
@@ -85,6 +93,7 @@ __global__ void __launch_bounds__(256) init_kernel(InitArgs A)
         double vx = A.vd0 + A.vth0 * (double)(ra * ca);
         const double vy = A.vd1 + A.vth1 * (double)(ra * sa);
         if (A.beam_v != 0.0) vx += (i & 1) ? -A.beam_v : A.beam_v;
+        vx += dvx;
         A.cell[i] = cx | (cy << 16);
         A.ox[i] = ox;
         A.oy[i] = oy;
@@ -185,6 +194,11 @@ pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_
     A.amp = spec->pert_amp;
     A.kx = 2.0 * 3.14159265358979323846 * spec->pert_mx / h->g.Lx;
     A.ky = 2.0 * 3.14159265358979323846 * spec->pert_my / h->g.Ly;
+    for (int b = 0; b < 2; ++b)
+        for (int c = 0; c < 2; ++c) {
+            A.xi[b][c] = spec->beam_xi[b][c];
+            A.uu[b][c] = spec->beam_u[b][c];
+        }
     A.k0 = (uint32_t)spec->seed;
     A.k1 = (uint32_t)(spec->seed >> 32);
     if (A.n > 0) {

@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(HERE, "libpic.so")
 MAX_SPECIES = 4
 SPECIES_HAS_VZ = 1
 LOAD_RANDOM, LOAD_LATTICE = 0, 1
-PERT_NONE, PERT_XDISP, PERT_DENSITY = 0, 1, 2
+PERT_NONE, PERT_XDISP, PERT_DENSITY, PERT_BEAM_MODE = 0, 1, 2, 3
 COLLIDE_MCC, COLLIDE_DSMC = 1, 2
 GRID_RHO, GRID_PHI, GRID_EX, GRID_EY = 0, 1, 2, 3
 HIST_FIELD_ENERGY, HIST_KINETIC, HIST_MOMENTUM_X, HIST_MOMENTUM_Y, HIST_CHARGE, HIST_MODE_AMP = range(6)
@@ -67,7 +67,8 @@ class InitSpec(C.Structure):
     _fields_ = [("n", C.c_longlong), ("layout", C.c_int), ("pert_kind", C.c_int),
                 ("vth", C.c_double * 3), ("vdrift", C.c_double * 2), ("beam_v", C.c_double),
                 ("pert_amp", C.c_double), ("pert_mx", C.c_int), ("pert_my", C.c_int),
-                ("seed", C.c_ulonglong)]
+                ("seed", C.c_ulonglong), ("beam_xi", (C.c_double * 2) * 2),
+                ("beam_u", (C.c_double * 2) * 2)]
 
 
 class Diag(C.Structure):
@@ -227,14 +228,44 @@ def config(nx, ny, Lx, Ly, dt, species_list, eps0=1.0, **tuning) -> Config:
 
 
 def init_spec(n, layout=LOAD_RANDOM, vth=(0.0, 0.0, 0.0), vdrift=(0.0, 0.0), beam_v=0.0,
-              pert_kind=PERT_NONE, pert_amp=0.0, pert_mx=0, pert_my=0, seed=0) -> InitSpec:
+              pert_kind=PERT_NONE, pert_amp=0.0, pert_mx=0, pert_my=0, seed=0,
+              beam_xi=((0, 0), (0, 0)), beam_u=((0, 0), (0, 0))) -> InitSpec:
     s = InitSpec()
     s.n, s.layout, s.pert_kind = int(n), layout, pert_kind
     for i in range(3):
         s.vth[i] = float(vth[i]) if i < len(vth) else 0.0
     s.vdrift[0], s.vdrift[1] = float(vdrift[0]), float(vdrift[1])
     s.beam_v, s.pert_amp, s.pert_mx, s.pert_my, s.seed = beam_v, pert_amp, pert_mx, pert_my, seed
+    for b in range(2):
+        for c in range(2):
+            s.beam_xi[b][c] = float(beam_xi[b][c])
+            s.beam_u[b][c] = float(beam_u[b][c])
     return s
+
+
+def two_stream_growing_mode(k, v0, omega_b2=0.5, amp=1e-4):
+    """Linear growing eigenmode of two symmetric cold beams (+v0, -v0), each
+    with plasma frequency^2 omega_b2, at wavenumber k (plasma units, q/m = -1).
+    Returns (gamma, beam_xi, beam_u) for PERT_BEAM_MODE, scaled so that the
+    total density perturbation has amplitude `amp` (relative)."""
+    n0 = 1.0  # per-beam density in units where omega_b2 = n0 * q^2 / m
+    M = np.zeros((4, 4), complex)
+    for j, v in enumerate((v0, -v0)):
+        M[j, j] = -1j * k * v
+        M[j, 2 + j] = -1j * k * n0
+        M[2 + j, 2 + j] = -1j * k * v
+        M[2 + j, 0] += omega_b2 / (1j * k)
+        M[2 + j, 1] += omega_b2 / (1j * k)
+    w, V = np.linalg.eig(M)
+    g = int(np.argmax(w.real))
+    vec = V[:, g]
+    # relative density of each beam n_b/n0; displacement xi = i n_b / (k n0)
+    scale = amp / abs(vec[0] + vec[1]) * 2.0
+    vec = vec * scale
+    xi = [1j * vec[j] / k for j in range(2)]
+    u = [vec[2 + j] for j in range(2)]
+    return (float(w[g].real), tuple((z.real, z.imag) for z in xi),
+            tuple((z.real, z.imag) for z in u))
 
 
 class Handle:

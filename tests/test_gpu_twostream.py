@@ -1,0 +1,105 @@
+"""Two-stream instability (BASELINE config 1: 128 x 128 cells, L = 4 pi,
+100 electrons per cell in two beams +-0.2, dt = 0.1, plasma units)."""
+import numpy as np
+import pytest
+
+import picgpu as P
+from gpu_util import normalized_electrons, oracle_from_handle
+
+pytestmark = pytest.mark.gpu
+
+NX = NY = 128
+L = 4 * np.pi
+PPC = 100
+N = NX * NY * PPC
+DT = 0.1
+V0 = 0.2
+K = 2 * np.pi / L  # mode 1: k = 0.5
+
+
+def linear_growth_rate(k, v0, wb2=0.5):
+    a = k * v0
+    w2 = a * a + wb2 - np.sqrt(wb2) * np.sqrt(wb2 + 4 * a * a)
+    return np.sqrt(-w2)
+
+
+@pytest.mark.parametrize("nx,ny,ppc", [(512, 4, 400), (128, 4, 1600)])
+def test_growth_rate_matches_linear_theory(nx, ny, ppc):
+    """Cold beams +-0.2 in the config-1 domain (Lx = 4 pi, dt = 0.1) on a quiet
+    (lattice) load, with the growing eigenmode of mode kx = 0.5 loaded:
+    |rho^(1,0)| must grow at the cold-beam rate
+    gamma = sqrt(-(a^2 + wb^2 - wb sqrt(wb^2 + 4 a^2))), a = k v0, within 2 %.
+    Quasi-1D (a few cells in y), so that the fast modes at other ky, seeded
+    only by rounding, stay small over the fitted window."""
+    gamma_th = linear_growth_rate(K, V0)
+    g, xi, u = P.two_stream_growing_mode(K, V0, amp=1e-6)
+    assert g == pytest.approx(gamma_th, rel=1e-9)
+    n = nx * ny * ppc
+    Ly = L * ny / nx
+    cfg, q, m = normalized_electrons(nx, ny, L, Ly, n, DT, sort_every=10)
+    nst = 400
+    with P.Handle(cfg) as h:
+        h.track_mode(1, 0)
+        h.init_particles(0, P.init_spec(n, layout=P.LOAD_LATTICE, beam_v=V0,
+                                        pert_kind=P.PERT_BEAM_MODE, pert_mx=1,
+                                        beam_xi=xi, beam_u=u, seed=0))
+        h.prime_leapfrog()
+        h.step(nst)
+        amp = h.history(P.HIST_MODE_AMP, 0, nst + 1)
+    t = np.arange(nst + 1) * DT
+    sel = (t >= 2.0) & (t <= 38.0)
+    gamma = np.polyfit(t[sel], np.log(amp[sel]), 1)[0]
+    print(f"{nx}x{ny} {ppc} ppc: measured gamma {gamma:.5f}, linear theory {gamma_th:.5f}")
+    assert gamma == pytest.approx(gamma_th, rel=0.02)
+    assert amp[sel][-1] / amp[sel][0] > 20  # the mode grew through the window
+
+
+def config1_spec(seed=0):
+    # x-displacement of amplitude 1e-3 in mode kx = 0.5, uniform random positions
+    return P.init_spec(N, layout=P.LOAD_RANDOM, vth=(0.01, 0.01, 0), beam_v=V0,
+                       pert_kind=P.PERT_XDISP, pert_amp=1e-3, pert_mx=1, seed=seed)
+
+
+def test_config1_matches_fp64_oracle_early_phase():
+    cfg, q, m = normalized_electrons(NX, NY, L, L, N, DT, sort_every=10)
+    nst = 100
+    with P.Handle(cfg) as h:
+        h.init_particles(0, config1_spec())
+        st = oracle_from_handle(h, cfg, q, m)
+        h.prime_leapfrog()
+        st.prime(nthreads=0)
+        h.step(nst)
+        fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
+        ke = h.history(P.HIST_KINETIC, 0, nst)
+        rho = h.grid(P.GRID_RHO)
+        ex = h.grid(P.GRID_EX)
+    ref = st.run(nst, nthreads=0)
+    err_fe = np.max(np.abs(fe - ref["fe"]) / ref["fe"])
+    err_ke = np.max(np.abs(ke - ref["ke"]) / ref["ke"])
+    print(f"field energy max rel err {err_fe:.2e}, kinetic {err_ke:.2e}")
+    assert err_fe < 1e-3
+    assert err_ke < 1e-5
+    np.testing.assert_allclose(rho, ref["rho"], atol=2e-3 * np.abs(ref["rho"]).max())
+    np.testing.assert_allclose(ex, ref["ex"], atol=2e-3 * np.abs(ref["ex"]).max())
+
+
+def test_config1_full_run_conserves_energy_and_charge():
+    cfg, q, m = normalized_electrons(NX, NY, L, L, N, DT, sort_every=10)
+    nst = 1000
+    with P.Handle(cfg) as h:
+        h.init_particles(0, config1_spec())
+        h.prime_leapfrog()
+        h.step(nst)
+        fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
+        ke = h.history(P.HIST_KINETIC, 0, nst)
+        qh = h.history(P.HIST_CHARGE, 0, nst + 1)
+        grids = [h.grid(k) for k in (P.GRID_RHO, P.GRID_PHI, P.GRID_EX, P.GRID_EY)]
+        d = h.diagnostics()
+    tot = fe[:-1] + ke
+    drift = np.ptp(tot) / tot[0]
+    print(f"total energy drift over 1000 steps {drift:.2e}; peak field energy {fe.max():.3e}")
+    assert drift < 0.02
+    # the instability grows and saturates: field energy rises by orders of magnitude
+    assert fe.max() > 50 * fe[0]
+    assert (qh == -N * 2.0**32).all() and d.error_flags == 0
+    assert all(np.isfinite(g).all() for g in grids)
