@@ -202,7 +202,67 @@ pic_status pic_poisson(pic_handle *h); /* rho -> E (cuFFT R2C, k-space kernel, C
 pic_status pic_gather_push(pic_handle *h, int deposit);
 
 enum pic_collide_kind { PIC_COLLIDE_MCC = 1, PIC_COLLIDE_DSMC = 2 };
+
+/* Electron-neutral Monte Carlo collisions against a uniform background gas,
+ * by the null-collision method (Vahedi & Surendra, Comput. Phys. Commun. 87
+ * (1995) 179): each step every electron is a candidate with probability
+ * P = 1 - exp(-nu_max dt), nu_max = n_g max_E sigma_T(E) v(E); a candidate's
+ * process follows from one uniform number against nu_j(E)/nu_max.
+ * Processes: elastic (isotropic, energy loss 2 m/M (1 - cos chi) E),
+ * excitation (E -= e_exc, isotropic), ionisation (E -= e_ion, the rest
+ * split uniformly between scattered and ejected electron, each isotropic; a
+ * new ion from the neutral Maxwellian at the same position).  Velocities
+ * are 3-D (species need PIC_SPECIES_HAS_VZ).  Random numbers: Philox4x32-10
+ * keyed by seed, counter (particle id, collision pass, stream).  Replaces
+ * the reference's constant-probability velocity resample
+ * (mccCollisions/src/particle.cc:112-127, mccCollisions/src/pic.cu:435-466). */
+typedef struct pic_mcc_params {
+    int electron_species;     /* species index of the electrons                 */
+    int ion_species;          /* species receiving ionisation ions (-1: none)   */
+    double neutral_density;   /* n_g, m^-3                                      */
+    double neutral_temp_eV;   /* background temperature (ion birth velocities)  */
+    double electron_mass;     /* physical electron mass, kg (energies)          */
+    double ion_mass;          /* physical ion / neutral mass, kg                */
+    double unit_charge;       /* C per eV                                       */
+    int ntab;                 /* table points, log-spaced in [e_min, e_max] eV  */
+    double e_min_eV, e_max_eV;
+    const double *sigma_elastic;    /* ntab cross sections, m^2 (copied)        */
+    const double *sigma_excitation;
+    const double *sigma_ionization;
+    double e_exc_eV, e_ion_eV; /* thresholds = energy losses                    */
+    unsigned long long seed;
+} pic_mcc_params;
+/* Configure MCC (once; the tables are copied).  pic_step then runs one MCC
+ * pass after each push; pic_collide(h, PIC_COLLIDE_MCC) runs one pass now. */
+pic_status pic_set_mcc(pic_handle *h, const pic_mcc_params *p);
+
+/* Neutral-neutral DSMC with Bird's no-time-counter scheme (Bird, Molecular
+ * Gas Dynamics and the Direct Simulation of Gas Flows, 1994), hard spheres:
+ * per cell of the cell-sorted array, N = 1/2 n (n-1) F_N (sigma g)_max dt_c
+ * / V_c candidate pairs (fraction by randomised rounding), each accepted
+ * with probability sigma g / (sigma g)_max, isotropic scattering in the
+ * centre-of-mass frame.  (sigma g)_max is kept per cell and raised when
+ * exceeded.  Replaces the reference's nearest-neighbour toy
+ * (dsmcCollisions/cellTrackerAdvanced/src/main.cc:288-350, src/pic.cu:791-870). */
+typedef struct pic_dsmc_params {
+    int species;              /* neutral species (q = 0, PIC_SPECIES_HAS_VZ)    */
+    double diameter;          /* hard-sphere diameter, m                        */
+    double weight;            /* F_N: real atoms per macro-particle             */
+    double depth;             /* cell depth for the 2-D cell volume, m          */
+    double sigma_g_max0;      /* initial (sigma g)_max per cell, m^3/s          */
+    int every;                /* collide every `every` steps, dt_c = every*dt (0: 1) */
+    unsigned long long seed;
+} pic_dsmc_params;
+pic_status pic_set_dsmc(pic_handle *h, const pic_dsmc_params *p);
+
+/* One collision pass now (MCC: on the live arrays; DSMC: sorts the neutral
+ * species by cell first). */
 pic_status pic_collide(pic_handle *h, int kind);
+
+/* Cumulative collision counts since init: [0] elastic, [1] excitation,
+ * [2] ionisation, [3] null candidates, [4] DSMC collisions,
+ * [5] DSMC candidate pairs. */
+pic_status pic_collision_counts(pic_handle *h, long long counts[6]);
 
 /* nsteps full steps (push+deposit, Poisson, sort every sort_every), replayed
  * from CUDA graphs.  Asynchronous: returns once the work is queued. */

@@ -96,6 +96,8 @@ static void free_handle_buffers(pic_handle *h)
     cudaFree(h->dev);
     cudaFree(h->hist);
     cudaFree(h->stage);
+    cudaFree(h->mcc.tab);
+    cudaFree(h->dsmc.sgmax);
     if (h->plan_r2c) cufftDestroy(h->plan_r2c);
     if (h->plan_c2r2) cufftDestroy(h->plan_c2r2);
     if (h->plan_c2r1) cufftDestroy(h->plan_c2r1);
@@ -121,7 +123,7 @@ static pic_status validate(const pic_config *c, pic_handle *h)
     };
     if (c->nx < 2 || c->ny < 2 || c->nx > 32768 || c->ny > 32768)
         return bad("nx, ny must be in [2, 32768]");
-    if ((long long)c->nx * c->ny > (1ll << 24)) return bad("nx*ny must be <= 2^24");
+    if ((long long)c->nx * c->ny > (1ll << 24) - 1) return bad("nx*ny must be < 2^24");
     if (!(c->Lx > 0) || !(c->Ly > 0) || !(c->dt > 0) || !(c->eps0 > 0))
         return bad("Lx, Ly, dt, eps0 must be positive");
     if (c->nspecies < 1 || c->nspecies > PIC_MAX_SPECIES) return bad("nspecies out of range");
@@ -215,11 +217,23 @@ static pic_status record_poisson(pic_handle *h)
     return PIC_OK;
 }
 
+// Particle pass of one step.  src = 1: every species was just sorted into
+// buffer 1.  A DSMC species is sorted every step and collides on its sorted
+// buffer before its push moves it back; MCC follows the push.
 static pic_status record_push_all(pic_handle *h, int src, bool deposit)
 {
-    for (int s = 0; s < h->cfg.nspecies; ++s)
-        if (h->sp[s].cap) PIC_TRY(launch_push(h, s, src, deposit, 1.0f));
+    for (int s = 0; s < h->cfg.nspecies; ++s) {
+        if (!h->sp[s].cap) continue;
+        int from = src;
+        if (h->dsmc.on && s == h->dsmc.s) {
+            if (!src) PIC_TRY(launch_sort(h, s));
+            PIC_TRY(launch_ntc(h));
+            from = 1;
+        }
+        PIC_TRY(launch_push(h, s, from, deposit, 1.0f));
+    }
     PIC_TRY(launch_advance(h, ADV_PUSH));
+    if (h->mcc.on) PIC_TRY(launch_mcc(h));
     return PIC_OK;
 }
 
@@ -230,10 +244,13 @@ static pic_status record_step(pic_handle *h, int src)
     return PIC_OK;
 }
 
+// Sort every species; the DSMC species goes last so that the cell offsets it
+// collides on are the ones left in the shared sort buffers.
 static pic_status record_sort_all(pic_handle *h)
 {
     for (int s = 0; s < h->cfg.nspecies; ++s)
-        if (h->sp[s].cap) PIC_TRY(launch_sort(h, s));
+        if (h->sp[s].cap && !(h->dsmc.on && s == h->dsmc.s)) PIC_TRY(launch_sort(h, s));
+    if (h->dsmc.on && h->sp[h->dsmc.s].cap) PIC_TRY(launch_sort(h, h->dsmc.s));
     return PIC_OK;
 }
 
@@ -499,10 +516,10 @@ pic_status pic_create(const pic_config *cfg, pic_handle **out)
     H_TRY(dalloc(&h->rhohat, nk));
     H_TRY(dalloc(&h->ehat, 2 * nk));
     H_TRY(dalloc(&h->e, 2 * ncell));
-    H_TRY(dalloc(&h->count, ncell));
-    H_TRY(dalloc(&h->offset, ncell + 1));
-    H_TRY(dalloc(&h->cursor, ncell));
-    h->scan_blocks = (int)((ncell + 4095) / 4096);
+    H_TRY(dalloc(&h->count, ncell + 1));
+    H_TRY(dalloc(&h->offset, ncell + 2));
+    H_TRY(dalloc(&h->cursor, ncell + 1));
+    h->scan_blocks = (int)((ncell + 1 + 4095) / 4096);
     H_TRY(dalloc(&h->bsum, (size_t)std::max(h->scan_blocks, 1)));
     H_TRY(dalloc(&h->dev, 1));
     H_TRY(dalloc(&h->hist, 6 * (size_t)h->hist_cap));
@@ -883,10 +900,129 @@ pic_status pic_get_rho_fixed(pic_handle *h, int64_t *out)
 
 }  // extern "C"
 
+extern "C" pic_status pic_set_mcc(pic_handle *h, const pic_mcc_params *p)
+{
+    PIC_TRY(need(h));
+    const pic_config &c = h->cfg;
+    auto bad = [](const char *m) {
+        set_error(std::string("pic_set_mcc: ") + m);
+        return PIC_ERR_INVALID_ARG;
+    };
+    if (!p) return bad("null parameters");
+    if (p->electron_species < 0 || p->electron_species >= c.nspecies ||
+        !h->sp[p->electron_species].vz[0])
+        return bad("electron species must exist and carry vz");
+    if (p->ion_species >= c.nspecies ||
+        (p->ion_species >= 0 && (!h->sp[p->ion_species].vz[0] || p->ion_species == p->electron_species)))
+        return bad("ion species must carry vz and differ from the electrons");
+    if (p->ntab < 2 || p->ntab > 4096 || !(p->e_min_eV > 0) || !(p->e_max_eV > p->e_min_eV) ||
+        !p->sigma_elastic || !p->sigma_excitation || !p->sigma_ionization)
+        return bad("cross-section table");
+    if (!(p->neutral_density > 0) || !(p->electron_mass > 0) || !(p->ion_mass > 0) ||
+        !(p->unit_charge > 0) || p->neutral_temp_eV < 0 || p->e_exc_eV < 0 || p->e_ion_eV < 0)
+        return bad("physical constants");
+    const int nt = p->ntab;
+    std::vector<float> tab(4 * (size_t)nt);
+    const double lr = std::log(p->e_max_eV / p->e_min_eV) / (nt - 1);
+    double nu_max = 0.0;
+    auto vel = [&](double e) { return std::sqrt(2.0 * e * p->unit_charge / p->electron_mass); };
+    for (int k = 0; k < nt; ++k) {
+        const double e = p->e_min_eV * std::exp(lr * k);
+        tab[k] = (float)e;
+        tab[nt + k] = (float)p->sigma_elastic[k];
+        tab[2 * nt + k] = (float)p->sigma_excitation[k];
+        tab[3 * nt + k] = (float)p->sigma_ionization[k];
+        if (p->sigma_elastic[k] < 0 || p->sigma_excitation[k] < 0 || p->sigma_ionization[k] < 0)
+            return bad("negative cross section");
+    }
+    // upper bound of n_g sigma_T(E) v(E) with sigma linear between table
+    // points: the larger endpoint cross section at the segment's top speed
+    for (int k = 0; k + 1 < nt; ++k) {
+        const double s0 = p->sigma_elastic[k] + p->sigma_excitation[k] + p->sigma_ionization[k];
+        const double s1 = p->sigma_elastic[k + 1] + p->sigma_excitation[k + 1] + p->sigma_ionization[k + 1];
+        nu_max = std::max(nu_max, std::max(s0, s1) * vel(p->e_min_eV * std::exp(lr * (k + 1))));
+    }
+    nu_max *= p->neutral_density * 1.0001;
+    MccState &M = h->mcc;
+    if (!M.tab || M.ntab != nt) {
+        cudaFree(M.tab);
+        M.tab = nullptr;
+        PIC_CUDA(cudaMalloc(&M.tab, tab.size() * sizeof(float)));
+    }
+    PIC_CUDA(cudaMemcpy(M.tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
+    M.ntab = nt;
+    M.e = p->electron_species;
+    M.i = p->ion_species;
+    M.ln_emin = (float)std::log(p->e_min_eV);
+    M.inv_dln = (float)(1.0 / lr);
+    M.half_me_over_e = (float)(0.5 * p->electron_mass / p->unit_charge);
+    M.ng = (float)p->neutral_density;
+    M.nu_max = (float)nu_max;
+    M.p_null = (float)(1.0 - std::exp(-nu_max * c.dt));
+    M.two_m_over_M = (float)(2.0 * p->electron_mass / p->ion_mass);
+    M.e_exc = (float)p->e_exc_eV;
+    M.e_ion = (float)p->e_ion_eV;
+    M.vth_ion = (float)std::sqrt(p->neutral_temp_eV * p->unit_charge / p->ion_mass);
+    M.seed = p->seed;
+    M.on = true;
+    drop_graphs(h);
+    return PIC_OK;
+}
+
+extern "C" pic_status pic_set_dsmc(pic_handle *h, const pic_dsmc_params *p)
+{
+    PIC_TRY(need(h));
+    if (!p || p->species < 0 || p->species >= h->cfg.nspecies || !h->sp[p->species].vz[0] ||
+        h->cfg.species[p->species].q != 0.0 || !(p->diameter > 0) || !(p->weight > 0) ||
+        !(p->depth > 0) || !(p->sigma_g_max0 > 0)) {
+        set_error("pic_set_dsmc: the species must be neutral and carry vz; diameter, weight, "
+                  "depth and sigma_g_max0 must be positive");
+        return PIC_ERR_INVALID_ARG;
+    }
+    DsmcState &D = h->dsmc;
+    const size_t ncell = (size_t)h->g.nx * h->g.ny;
+    if (!D.sgmax) PIC_CUDA(cudaMalloc(&D.sgmax, ncell * sizeof(float)));
+    std::vector<float> init(ncell, (float)p->sigma_g_max0);
+    PIC_CUDA(cudaMemcpy(D.sgmax, init.data(), ncell * sizeof(float), cudaMemcpyHostToDevice));
+    D.s = p->species;
+    D.sigma = (float)(3.14159265358979323846 * p->diameter * p->diameter);
+    D.coef = (float)(p->weight * h->cfg.dt / (2.0 * h->g.dx * h->g.dy * p->depth));
+    D.seed = p->seed;
+    D.on = true;
+    drop_graphs(h);
+    return PIC_OK;
+}
+
 extern "C" pic_status pic_collide(pic_handle *h, int kind)
 {
     PIC_TRY(need(h));
-    set_error("pic_collide: no collision operator for this kind in this build");
-    (void)kind;
+    if (kind == PIC_COLLIDE_MCC) {
+        if (!h->mcc.on) {
+            set_error("pic_collide: MCC not configured (pic_set_mcc)");
+            return PIC_ERR_STATE;
+        }
+        return launch_mcc(h);
+    }
+    if (kind == PIC_COLLIDE_DSMC) {
+        if (!h->dsmc.on) {
+            set_error("pic_collide: DSMC not configured (pic_set_dsmc)");
+            return PIC_ERR_STATE;
+        }
+        PIC_TRY(launch_sort(h, h->dsmc.s));
+        PIC_TRY(launch_ntc(h));
+        return copy_back(h, h->dsmc.s);
+    }
+    set_error("pic_collide: unknown collision kind");
     return PIC_ERR_INVALID_ARG;
+}
+
+extern "C" pic_status pic_collision_counts(pic_handle *h, long long counts[6])
+{
+    PIC_TRY(need(h));
+    if (!counts) return PIC_ERR_INVALID_ARG;
+    PIC_CUDA(cudaStreamSynchronize(h->stream));
+    unsigned long long c[6];
+    PIC_CUDA(cudaMemcpy(c, h->dev->coll, sizeof c, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 6; ++k) counts[k] = (long long)c[k];
+    return PIC_OK;
 }

@@ -104,6 +104,28 @@ struct DevState {
     long long n[PIC_MAX_SPECIES];
     unsigned int err;         // PIC_DEVERR_* bits
     unsigned int pad;
+    unsigned long long coll[6];  // elastic, excitation, ionisation, null, DSMC collisions, pairs
+    unsigned long long mcc_pass, dsmc_pass;  // collision pass counters (Philox counters)
+    long long mcc_n0;         // electron count at the start of the current MCC pass
+};
+
+// MCC configuration resolved for the device
+struct MccState {
+    bool on = false;
+    int e = 0, i = -1;        // electron / ion species
+    float *tab = nullptr;     // device [energy | elastic | excitation | ionisation] x ntab
+    int ntab = 0;
+    float ln_emin = 0, inv_dln = 0, half_me_over_e = 0, ng = 0, nu_max = 0, p_null = 0;
+    float two_m_over_M = 0, e_exc = 0, e_ion = 0, vth_ion = 0;
+    unsigned long long seed = 0;
+};
+
+struct DsmcState {
+    bool on = false;
+    int s = 0;
+    float *sgmax = nullptr;   // per cell key
+    float sigma = 0, coef = 0;
+    unsigned long long seed = 0;
 };
 
 struct Geometry {
@@ -148,6 +170,9 @@ struct pic_handle {
     // host<->device staging for imports and exports (grown on demand)
     void *stage = nullptr;
     size_t stage_bytes = 0;
+    // collision operators
+    pic::MccState mcc;
+    pic::DsmcState dsmc;
 };
 
 namespace pic {
@@ -163,6 +188,9 @@ enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s);
+// pic_collide.cu
+pic_status launch_mcc(pic_handle *h);
+pic_status launch_ntc(pic_handle *h);
 // pic_init.cu
 pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_nx, int lat_ny);
 pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x_dev,

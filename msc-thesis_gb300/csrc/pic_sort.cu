@@ -50,15 +50,18 @@ constexpr int SORT_PER_THREAD = 16;
 constexpr int SORT_CHUNK = SORT_THREADS * SORT_PER_THREAD;
 constexpr int SORT_KEYS = 2048;
 
-// key of particle i, or -1 for an empty slot or a corrupt cell (flagged)
+// key of particle i; empty slots (cell < 0) inside [0, n) get the extra key
+// ncell so that they sort to the end and keep their slot count; a corrupt
+// cell is flagged and treated the same way
 __device__ __forceinline__ int particle_key(const SortArgs &A, long long i)
 {
     const int c = A.cin[i];
-    if (c < 0) return -1;
+    const int empty = A.nx * A.ny;
+    if (c < 0) return empty;
     const int cx = c & 0xFFFF, cy = c >> 16;
     if (cx >= A.nx || cy >= A.ny) {
         atomicOr(A.err, (unsigned)PIC_DEVERR_CELL);
-        return -1;
+        return empty;
     }
     return cell_key(c, A.tw, A.th, A.ntx);
 }
@@ -88,7 +91,6 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
         const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
         if (i >= n) break;
         const int key = particle_key(A, i);
-        if (key < 0) continue;
         const unsigned r = (unsigned)(key - k0);
         if (r < (unsigned)SORT_KEYS)
             atomicAdd(s_cnt + r, 1u);
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
     __syncthreads();
     for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) {
         const uint32_t v = s_cnt[r];
-        if (v && k0 + r < ncell) atomicAdd(A.count + k0 + r, v);
+        if (v && k0 + r <= ncell) atomicAdd(A.count + k0 + r, v);
     }
 }
 
@@ -232,7 +234,9 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_scatter_kernel(SortArgs A)
         keys[j] = -1;
         if (i < n) {
             const int c = A.cin[i];
-            if (c >= 0 && (c & 0xFFFF) < A.nx && (c >> 16) < A.ny) keys[j] = cell_key(c, A.tw, A.th, A.ntx);
+            keys[j] = (c >= 0 && (c & 0xFFFF) < A.nx && (c >> 16) < A.ny)
+                          ? cell_key(c, A.tw, A.th, A.ntx)
+                          : (int)ncell;
         }
         const unsigned r = (unsigned)(keys[j] - k0);
         if (keys[j] >= 0 && r < (unsigned)SORT_KEYS) atomicAdd(s_cnt + r, 1u);
@@ -241,7 +245,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_scatter_kernel(SortArgs A)
     // reserve each distinct key's slice of the output once per block
     for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) {
         const uint32_t v = s_cnt[r];
-        s_base[r] = (v && k0 + r < ncell) ? atomicAdd(A.cursor + k0 + r, v) : 0u;
+        s_base[r] = (v && k0 + r <= ncell) ? atomicAdd(A.cursor + k0 + r, v) : 0u;
         s_cnt[r] = 0u;
     }
     __syncthreads();
@@ -293,16 +297,17 @@ pic_status launch_sort(pic_handle *h, int s)
     A.ntx = g.ntx;
     A.chunk = g.chunk;
     A.err = &h->dev->err;
-    PIC_CUDA(cudaMemsetAsync(h->count, 0, sizeof(uint32_t) * (size_t)ncell, h->stream));
+    const long long nkeys = ncell + 1;  // cells + the bin of empty slots
+    PIC_CUDA(cudaMemsetAsync(h->count, 0, sizeof(uint32_t) * (size_t)nkeys, h->stream));
     PIC_CUDA(cudaMemsetAsync(B.anchor, 0xFF, sizeof(int32_t) * (size_t)B.nchunks, h->stream));
     const unsigned gp = (unsigned)((B.cap + SORT_CHUNK - 1) / SORT_CHUNK);
     sort_hist_kernel<<<gp, SORT_THREADS, 0, h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
-    scan_blocks_kernel<<<h->scan_blocks, 1024, 0, h->stream>>>(h->count, h->offset, ncell, h->bsum);
+    scan_blocks_kernel<<<h->scan_blocks, 1024, 0, h->stream>>>(h->count, h->offset, nkeys, h->bsum);
     PIC_CUDA(cudaGetLastError());
     scan_bsum_kernel<<<1, 1024, 0, h->stream>>>(h->bsum, h->scan_blocks);
     PIC_CUDA(cudaGetLastError());
-    scan_add_kernel<<<grid_for(ncell, 256), 256, 0, h->stream>>>(h->offset, h->cursor, ncell,
+    scan_add_kernel<<<grid_for(nkeys, 256), 256, 0, h->stream>>>(h->offset, h->cursor, nkeys,
                                                                h->bsum, &h->dev->n[s]);
     PIC_CUDA(cudaGetLastError());
     sort_scatter_kernel<<<gp, SORT_THREADS, 0, h->stream>>>(A);

@@ -78,6 +78,22 @@ class Diag(C.Structure):
                 ("n", C.c_longlong * MAX_SPECIES), ("error_flags", C.c_uint)]
 
 
+class MccParams(C.Structure):
+    _fields_ = [("electron_species", C.c_int), ("ion_species", C.c_int),
+                ("neutral_density", C.c_double), ("neutral_temp_eV", C.c_double),
+                ("electron_mass", C.c_double), ("ion_mass", C.c_double),
+                ("unit_charge", C.c_double), ("ntab", C.c_int), ("e_min_eV", C.c_double),
+                ("e_max_eV", C.c_double), ("sigma_elastic", C.POINTER(C.c_double)),
+                ("sigma_excitation", C.POINTER(C.c_double)),
+                ("sigma_ionization", C.POINTER(C.c_double)), ("e_exc_eV", C.c_double),
+                ("e_ion_eV", C.c_double), ("seed", C.c_ulonglong)]
+
+
+class DsmcParams(C.Structure):
+    _fields_ = [("species", C.c_int), ("diameter", C.c_double), ("weight", C.c_double),
+                ("depth", C.c_double), ("sigma_g_max0", C.c_double), ("seed", C.c_ulonglong)]
+
+
 class ParticlesView(C.Structure):
     _fields_ = [("n", C.c_longlong), ("cell_dev", C.c_void_p), ("ox_dev", C.c_void_p),
                 ("oy_dev", C.c_void_p), ("vx_dev", C.c_void_p), ("vy_dev", C.c_void_p),
@@ -112,6 +128,9 @@ SIGNATURES = {
     "pic_poisson": [_H],
     "pic_gather_push": [_H, C.c_int],
     "pic_collide": [_H, C.c_int],
+    "pic_set_mcc": [_H, C.POINTER(MccParams)],
+    "pic_set_dsmc": [_H, C.POINTER(DsmcParams)],
+    "pic_collision_counts": [_H, _vp],
     "pic_step": [_H, C.c_longlong],
     "pic_run_host": [_H, C.c_longlong, _vp, _vp, _vp, _vp, C.c_longlong, C.c_int,
                      _vp, _vp, _vp, _vp],
@@ -355,6 +374,25 @@ class Handle:
 
     def step(self, n=1):
         self._c("pic_step", int(n))
+
+    def set_mcc(self, electron_species, ion_species, neutral_density, neutral_temp_eV,
+                electron_mass, ion_mass, unit_charge, e_min_eV, e_max_eV, sigma_elastic,
+                sigma_excitation, sigma_ionization, e_exc_eV, e_ion_eV, seed=0):
+        tabs = [_f64(t) for t in (sigma_elastic, sigma_excitation, sigma_ionization)]
+        self._mcc_tabs = tabs
+        p = MccParams(electron_species, ion_species, neutral_density, neutral_temp_eV,
+                      electron_mass, ion_mass, unit_charge, len(tabs[0]), e_min_eV, e_max_eV,
+                      *[t.ctypes.data_as(_dp) for t in tabs], e_exc_eV, e_ion_eV, seed)
+        self._c("pic_set_mcc", C.byref(p))
+
+    def set_dsmc(self, species, diameter, weight, depth, sigma_g_max0, seed=0):
+        p = DsmcParams(species, diameter, weight, depth, sigma_g_max0, seed)
+        self._c("pic_set_dsmc", C.byref(p))
+
+    def collision_counts(self):
+        c = np.zeros(6, dtype=np.int64)
+        self._c("pic_collision_counts", _ptr(c))
+        return c
 
     def synchronize(self):
         self._c("pic_synchronize")

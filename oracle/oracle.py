@@ -211,3 +211,57 @@ def deposit_fixed(nx, ny, cell, ox, oy, q_int=1, rho=None):
     lib().orc_deposit_fixed(nx, ny, len(cell), cell.ctypes.data, ox.ctypes.data, oy.ctypes.data,
                             int(q_int), rho.ctypes.data)
     return rho
+
+
+# ------------------------------------------------------------- collisions ----
+class MccC(C.Structure):
+    _fields_ = [("ntab", C.c_int), ("e_min", C.c_double), ("e_max", C.c_double),
+                ("sel", _dp), ("sexc", _dp), ("sion", _dp), ("ng", C.c_double),
+                ("half_me_over_e", C.c_double), ("two_m_over_M", C.c_double),
+                ("e_exc", C.c_double), ("e_ion", C.c_double), ("vth_ion", C.c_double),
+                ("nu_max", C.c_double), ("p_null", C.c_double), ("seed", C.c_uint64)]
+
+
+class DsmcC(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("Lx", C.c_double), ("Ly", C.c_double),
+                ("dt", C.c_double), ("sigma", C.c_double), ("coef", C.c_double),
+                ("mass", C.c_double), ("seed", C.c_uint64)]
+
+
+def mcc_pass(m: dict, pid, vx, vy, vz, pass_no, cap_new=None):
+    """One MCC pass (restatement).  m: dict with the MccC fields, tables as
+    numpy arrays.  Returns (vx, vy, vz, new_e (k,3), new_i (k,3), parent, counts)."""
+    L = lib()
+    L.orc_mcc_pass.restype = C.c_long
+    L.orc_mcc_pass.argtypes = [C.POINTER(MccC), C.c_long, C.c_void_p, _dp, _dp, _dp, C.c_uint64,
+                               C.c_long, _dp, _dp, C.c_void_p, C.c_void_p]
+    tabs = [np.ascontiguousarray(m[k], dtype=np.float64) for k in ("sel", "sexc", "sion")]
+    mc = MccC(len(tabs[0]), m["e_min"], m["e_max"], *[_p(t) for t in tabs], m["ng"],
+              m["half_me_over_e"], m["two_m_over_M"], m["e_exc"], m["e_ion"], m["vth_ion"],
+              m["nu_max"], m["p_null"], m["seed"])
+    vx, vy, vz = (np.array(a, dtype=np.float64) for a in (vx, vy, vz))
+    pid = np.ascontiguousarray(pid, dtype=np.uint32)
+    n = len(vx)
+    cap = n if cap_new is None else cap_new
+    ne, ni = np.zeros((cap, 3)), np.zeros((cap, 3))
+    parent = np.zeros(cap, dtype=np.int64)
+    counts = np.zeros(4, dtype=np.int64)
+    born = L.orc_mcc_pass(C.byref(mc), n, pid.ctypes.data, _p(vx), _p(vy), _p(vz), pass_no, cap,
+                          _p(ne), _p(ni), parent.ctypes.data, counts.ctypes.data)
+    return vx, vy, vz, ne[:born], ni[:born], parent[:born], counts
+
+
+def dsmc_run(d: dict, x, y, vx, vy, vz, sgmax, nsteps, first_pass=0):
+    L = lib()
+    L.orc_dsmc_run.restype = None
+    L.orc_dsmc_run.argtypes = [C.POINTER(DsmcC), C.c_long, _dp, _dp, _dp, _dp, _dp, _dp,
+                               C.c_long, C.c_uint64, _dp, _dp, C.c_void_p]
+    dc = DsmcC(d["nx"], d["ny"], d["Lx"], d["Ly"], d["dt"], d["sigma"], d["coef"], d["mass"],
+               d["seed"])
+    x, y, vx, vy, vz = (np.array(a, dtype=np.float64) for a in (x, y, vx, vy, vz))
+    sg = np.array(sgmax, dtype=np.float64)
+    te, to = np.zeros(nsteps), np.zeros(nsteps)
+    counts = np.zeros(2, dtype=np.int64)
+    L.orc_dsmc_run(C.byref(dc), len(x), _p(x), _p(y), _p(vx), _p(vy), _p(vz), _p(sg), nsteps,
+                   first_pass, _p(te), _p(to), counts.ctypes.data)
+    return dict(x=x, y=y, vx=vx, vy=vy, vz=vz, T_even=te, T_odd=to, counts=counts)

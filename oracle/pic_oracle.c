@@ -634,3 +634,230 @@ void orc_deposit_fixed(int nx, int ny, long n, const int32_t *cell, const float 
         rho[(size_t)iy1 * nx + ix1] += q_int * (int64_t)(fx * fy);
     }
 }
+
+/* ===================================================================== */
+/* Part 4: collision operators, restated from pic_collide.cu.            */
+/* ===================================================================== */
+#define STREAM_MCC 0x6d636321u
+#define STREAM_DSMC 0x64736d63u
+
+static double u24(uint32_t r) { return ((double)(r >> 8) + 0.5) * (1.0 / 16777216.0); }
+
+static void philox_u4(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint64_t seed, uint32_t o[4])
+{
+    uint32_t c[4] = {c0, c1, c2, c3};
+    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    orc_philox4x32_10(c, k, o);
+}
+
+/* orthonormal basis perpendicular to u (Duff et al., JCGT 6(1), 2017) */
+static void deflect(double ux, double uy, double uz, double c, double w, double out[3])
+{
+    double sgn = uz >= 0.0 ? 1.0 : -1.0;
+    double a = -1.0 / (sgn + uz);
+    double b = ux * uy * a;
+    double e1[3] = {1.0 + sgn * ux * ux * a, sgn * b, -sgn * ux};
+    double e2[3] = {b, sgn + uy * uy * a, -uy};
+    double s = sqrt(fmax(0.0, 1.0 - c * c));
+    double cp = cos(2.0 * M_PI * w), sp = sin(2.0 * M_PI * w);
+    for (int i = 0; i < 3; ++i) out[i] = c * (i == 0 ? ux : i == 1 ? uy : uz) + s * (cp * e1[i] + sp * e2[i]);
+}
+
+static void mcc_sigmas(const orc_mcc *m, double E, double *sel, double *sexc, double *sion)
+{
+    int nt = m->ntab;
+    double lr = log(m->e_max / m->e_min) / (nt - 1);
+    int k;
+    double f, e0, e1;
+    if (E <= m->e_min) {
+        k = 0;
+        f = 0.0;
+    } else if (E >= m->e_max) {
+        k = nt - 2;
+        f = 1.0;
+    } else {
+        k = (int)(log(E / m->e_min) / lr);
+        if (k < 0) k = 0;
+        if (k > nt - 2) k = nt - 2;
+        e0 = m->e_min * exp(lr * k);
+        e1 = m->e_min * exp(lr * (k + 1));
+        if (E < e0 && k > 0) {
+            --k;
+            e1 = e0;
+            e0 = m->e_min * exp(lr * k);
+        }
+        if (E >= e1 && k < nt - 2) {
+            ++k;
+            e0 = e1;
+            e1 = m->e_min * exp(lr * (k + 1));
+        }
+        f = (E - e0) / (e1 - e0);
+    }
+    *sel = m->sel[k] + f * (m->sel[k + 1] - m->sel[k]);
+    *sexc = m->sexc[k] + f * (m->sexc[k + 1] - m->sexc[k]);
+    *sion = m->sion[k] + f * (m->sion[k + 1] - m->sion[k]);
+}
+
+long orc_mcc_pass(const orc_mcc *m, long n, const uint32_t *pid, double *vx, double *vy,
+                  double *vz, uint64_t pass, long cap_new, double *new_e, double *new_i,
+                  long *parent, long counts[4])
+{
+    long born = 0;
+    for (long i = 0; i < n; ++i) {
+        uint32_t r[4];
+        philox_u4(pid[i], (uint32_t)pass, 0u, STREAM_MCC, m->seed, r);
+        if (u24(r[0]) >= m->p_null) continue;
+        double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        double v = sqrt(v2), E = m->half_me_over_e * v2;
+        double sel, sexc, sion;
+        mcc_sigmas(m, E, &sel, &sexc, &sion);
+        if (E < m->e_exc) sexc = 0.0;
+        if (E < m->e_ion) sion = 0.0;
+        double nel = m->ng * sel * v, nexc = m->ng * sexc * v, nion = m->ng * sion * v;
+        double R = u24(r[1]) * m->nu_max;
+        double ux = v > 0 ? vx[i] / v : 0.0, uy = v > 0 ? vy[i] / v : 0.0, uz = v > 0 ? vz[i] / v : 1.0;
+        double d[3], vn;
+        if (R < nel) {
+            double c = 1.0 - 2.0 * u24(r[2]);
+            double En = E * (1.0 - m->two_m_over_M * (1.0 - c));
+            deflect(ux, uy, uz, c, u24(r[3]), d);
+            vn = sqrt(En / m->half_me_over_e);
+            counts[0]++;
+        } else if (R < nel + nexc) {
+            deflect(ux, uy, uz, 1.0 - 2.0 * u24(r[2]), u24(r[3]), d);
+            vn = sqrt(fmax(E - m->e_exc, 0.0) / m->half_me_over_e);
+            counts[1]++;
+        } else if (R < nel + nexc + nion) {
+            uint32_t r2[4], r3[4];
+            philox_u4(pid[i], (uint32_t)pass, 1u, STREAM_MCC, m->seed, r2);
+            double Er = fmax(E - m->e_ion, 0.0), Ej = u24(r2[0]) * Er, Es = Er - Ej;
+            double dj[3];
+            deflect(ux, uy, uz, 1.0 - 2.0 * u24(r[2]), u24(r[3]), d);
+            deflect(ux, uy, uz, 1.0 - 2.0 * u24(r2[1]), u24(r2[2]), dj);
+            vn = sqrt(Es / m->half_me_over_e);
+            double vj = sqrt(Ej / m->half_me_over_e);
+            counts[2]++;
+            if (born < cap_new) {
+                philox_u4(pid[i], (uint32_t)pass, 2u, STREAM_MCC, m->seed, r3);
+                double ra = sqrt(-2.0 * log(u24(r3[0]))), rb = sqrt(-2.0 * log(u24(r3[2])));
+                for (int k = 0; k < 3; ++k) new_e[3 * born + k] = vj * dj[k];
+                new_i[3 * born + 0] = m->vth_ion * ra * cos(2.0 * M_PI * u24(r3[1]));
+                new_i[3 * born + 1] = m->vth_ion * ra * sin(2.0 * M_PI * u24(r3[1]));
+                new_i[3 * born + 2] = m->vth_ion * rb * cos(2.0 * M_PI * u24(r3[3]));
+                parent[born] = i;
+                born++;
+            }
+        } else {
+            counts[3]++;
+            continue;
+        }
+        vx[i] = vn * d[0];
+        vy[i] = vn * d[1];
+        vz[i] = vn * d[2];
+    }
+    return born;
+}
+
+static void group_temps(long n, const double *vx, const double *vy, const double *vz, double mass,
+                        double *te, double *to)
+{
+    double s[2][3] = {{0}}, q[2] = {0}, c[2] = {0};
+    for (long i = 0; i < n; ++i) {
+        int g = (int)(i & 1);
+        s[g][0] += vx[i];
+        s[g][1] += vy[i];
+        s[g][2] += vz[i];
+        q[g] += vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        c[g] += 1.0;
+    }
+    const double kB = 1.380649e-23;
+    for (int g = 0; g < 2; ++g) {
+        double m2 = 0.0;
+        for (int k = 0; k < 3; ++k) m2 += (s[g][k] / c[g]) * (s[g][k] / c[g]);
+        double T = mass * (q[g] / c[g] - m2) / (3.0 * kB);
+        if (g == 0 && te) *te = T;
+        if (g == 1 && to) *to = T;
+    }
+}
+
+void orc_dsmc_run(const orc_dsmc *d, long n, double *x, double *y, double *vx, double *vy,
+                  double *vz, double *sgmax, long nsteps, uint64_t first_pass, double *T_even,
+                  double *T_odd, long counts[2])
+{
+    const int nx = d->nx, ny = d->ny;
+    const long nc = (long)nx * ny;
+    const double dx = d->Lx / nx, dy = d->Ly / ny;
+    long *cnt = (long *)calloc((size_t)nc + 1, sizeof(long));
+    long *idx = (long *)malloc(sizeof(long) * (size_t)(n > 0 ? n : 1));
+    long *cell = (long *)malloc(sizeof(long) * (size_t)(n > 0 ? n : 1));
+    for (long st = 0; st < nsteps; ++st) {
+        const uint64_t pass = first_pass + (uint64_t)st;
+        memset(cnt, 0, sizeof(long) * ((size_t)nc + 1));
+        for (long i = 0; i < n; ++i) {
+            long cx = (long)floor(x[i] / dx), cy = (long)floor(y[i] / dy);
+            if (cx >= nx) cx = nx - 1;
+            if (cy >= ny) cy = ny - 1;
+            if (cx < 0) cx = 0;
+            if (cy < 0) cy = 0;
+            cell[i] = cx + cy * nx;
+            cnt[cell[i] + 1]++;
+        }
+        for (long c = 0; c < nc; ++c) cnt[c + 1] += cnt[c];
+        {
+            long *pos = (long *)malloc(sizeof(long) * (size_t)nc);
+            memcpy(pos, cnt, sizeof(long) * (size_t)nc);
+            for (long i = 0; i < n; ++i) idx[pos[cell[i]]++] = i;
+            free(pos);
+        }
+        for (long c = 0; c < nc; ++c) {
+            long o0 = cnt[c], m = cnt[c + 1] - o0;
+            if (m < 2) continue;
+            double sgm = sgmax[c];
+            double want = d->coef * (double)m * (double)(m - 1) * sgm;
+            uint32_t r0[4];
+            philox_u4((uint32_t)c, (uint32_t)pass, 0u, STREAM_DSMC, d->seed, r0);
+            double fl = floor(want);
+            long ncand = (long)fl + (u24(r0[0]) < want - fl ? 1 : 0);
+            for (long k = 0; k < ncand; ++k) {
+                uint32_t r[4], r2[4];
+                philox_u4((uint32_t)c, (uint32_t)pass, (uint32_t)(2 * k + 1), STREAM_DSMC, d->seed, r);
+                long a = (long)(u24(r[0]) * m);
+                if (a > m - 1) a = m - 1;
+                long b = (long)(u24(r[1]) * (m - 1));
+                if (b > m - 2) b = m - 2;
+                if (b >= a) ++b;
+                long i = idx[o0 + a], j = idx[o0 + b];
+                double gx = vx[i] - vx[j], gy = vy[i] - vy[j], gz = vz[i] - vz[j];
+                double g = sqrt(gx * gx + gy * gy + gz * gz), sg = d->sigma * g;
+                if (sg > sgm) sgm = sg;
+                counts[1]++;
+                if (u24(r[2]) * sgm >= sg) continue;
+                philox_u4((uint32_t)c, (uint32_t)pass, (uint32_t)(2 * k + 2), STREAM_DSMC, d->seed, r2);
+                double cx_ = 2.0 * u24(r[3]) - 1.0, sx = sqrt(fmax(0.0, 1.0 - cx_ * cx_));
+                double ph = 2.0 * M_PI * u24(r2[0]);
+                double hx = 0.5 * g * cx_, hy = 0.5 * g * sx * cos(ph), hz = 0.5 * g * sx * sin(ph);
+                double mx = 0.5 * (vx[i] + vx[j]), my = 0.5 * (vy[i] + vy[j]), mz = 0.5 * (vz[i] + vz[j]);
+                vx[i] = mx + hx;
+                vy[i] = my + hy;
+                vz[i] = mz + hz;
+                vx[j] = mx - hx;
+                vy[j] = my - hy;
+                vz[j] = mz - hz;
+                counts[0]++;
+            }
+            sgmax[c] = sgm;
+        }
+        for (long i = 0; i < n; ++i) {
+            x[i] += vx[i] * d->dt;
+            y[i] += vy[i] * d->dt;
+            x[i] -= d->Lx * floor(x[i] / d->Lx);
+            y[i] -= d->Ly * floor(y[i] / d->Ly);
+            if (x[i] >= d->Lx) x[i] -= d->Lx;
+            if (y[i] >= d->Ly) y[i] -= d->Ly;
+        }
+        group_temps(n, vx, vy, vz, d->mass, T_even ? &T_even[st] : NULL, T_odd ? &T_odd[st] : NULL);
+    }
+    free(cnt);
+    free(idx);
+    free(cell);
+}

@@ -92,6 +92,44 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 void orc_deposit_fixed(int nx, int ny, long n, const int32_t *cell, const float *ox,
                        const float *oy, int64_t q_int, int64_t *rho);
 
+/* ---------------- collision operators (restatements of pic_collide.cu) ----
+ * Same algorithms, same Philox counters and the same 24-bit uniform
+ * conversion as the GPU, in double precision.  MCC draws are keyed by
+ * (particle id, pass, stream); the i-th candidate's decisions therefore
+ * match the GPU's except where a float comparison lands on the other side. */
+typedef struct orc_mcc {
+    int ntab;
+    double e_min, e_max;
+    const double *sel, *sexc, *sion;
+    double ng, half_me_over_e, two_m_over_M, e_exc, e_ion, vth_ion;
+    double nu_max, p_null; /* as the GPU uses them (float-rounded by the caller) */
+    uint64_t seed;
+} orc_mcc;
+
+/* One MCC pass over n electrons (velocities in/out).  Ionisations append
+ * the ejected electron's velocity to new_e[3*k..] and the ion's to
+ * new_i[3*k..] (k < cap_new) and the parent's index to parent[k].
+ * counts: elastic, excitation, ionisation, null.  Returns new pairs. */
+long orc_mcc_pass(const orc_mcc *m, long n, const uint32_t *pid, double *vx, double *vy,
+                  double *vz, uint64_t pass, long cap_new, double *new_e, double *new_i,
+                  long *parent, long counts[4]);
+
+/* DSMC (hard spheres, Bird's NTC) of one neutral species with free
+ * streaming, nsteps steps: each step groups particles by cell (cx + cy*nx),
+ * collides per cell, then moves x += v dt (periodic).  sgmax: per cell,
+ * in/out.  T_even / T_odd (may be NULL): temperature (kelvin, 3-D) of the
+ * particles with even / odd id after each step, kB T = m <|v - <v>|^2> / 3.
+ * counts[0] collisions, counts[1] candidate pairs. */
+typedef struct orc_dsmc {
+    int nx, ny;
+    double Lx, Ly, dt, sigma, coef; /* coef = F_N dt / (2 V_c) */
+    double mass;                    /* physical mass (temperatures) */
+    uint64_t seed;
+} orc_dsmc;
+void orc_dsmc_run(const orc_dsmc *d, long n, double *x, double *y, double *vx, double *vy,
+                  double *vz, double *sgmax, long nsteps, uint64_t first_pass, double *T_even,
+                  double *T_odd, long counts[2]);
+
 #ifdef __cplusplus
 }
 #endif
