@@ -204,6 +204,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--tile", type=int, nargs=2, default=(0, 0))
     ap.add_argument("--sort-every", type=int, default=SORT_EVERY)
+    ap.add_argument("--push-variant", type=int, default=0, help="0 auto, 1 direct, 2 bulk copy")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (untimed setup)")
     args = ap.parse_args()
     NX = NY = args.nx
     N = NX * NY * PPC
@@ -236,10 +238,18 @@ def main():
     A = L * L
     sp = P.species(N, -A / N, A / N, -1)
     cfg = P.config(NX, NY, L, L, DT, [sp], sort_every=SORT_EVERY, device=local,
-                   chunk=args.chunk, tile_w=args.tile[0], tile_h=args.tile[1])
-    h = P.Handle(cfg)
+                   chunk=args.chunk, tile_w=args.tile[0], tile_h=args.tile[1],
+                   push_variant=args.push_variant)
     spec = P.init_spec(N, vth=(VTH, VTH, 0), pert_kind=P.PERT_DENSITY, pert_amp=0.01,
                        pert_mx=1, pert_my=1, seed=2024 + rank)
+    tuned = None
+    if not args.no_tune and not args.chunk and not args.tile[0]:
+        # untimed setup: pick push chunk, tile and sort cadence on this workload
+        r = P.autotune(cfg, 0, spec, trial_steps=40)
+        tuned = {"chunk": r.chunk, "tile": [r.tile_w, r.tile_h], "sort_every": r.sort_every,
+                 "trial_ms_per_step": r.ms_per_step, "candidates": r.tried}
+        SORT_EVERY = r.sort_every
+    h = P.Handle(cfg)
     h.init_particles(0, spec)
     h.prime_leapfrog()
     stream = torch.cuda.ExternalStream(h.stream())
@@ -331,6 +341,7 @@ def main():
                        "hbm_frac_step": step_bytes * args.steps / (ms_max / 1000.0) / 1e9 / hbm,
                        "peak_kind": peak_kind,
                        "charge_exact": diag.total_charge_fixed == diag.expected_charge_fixed,
+                       "autotuned": tuned,
                        "field_energy": diag.field_energy},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": TRAFFIC_PER_PARTICLE * N,

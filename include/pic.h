@@ -123,6 +123,7 @@ typedef struct pic_config {
     int halo;            /* shared-memory window halo in cells (0: 2)         */
     int history;         /* diagnostic history length in steps (0: 4096)      */
     int device;          /* CUDA device ordinal                               */
+    int push_variant;    /* 0: auto, 1: direct 128-bit loads, 2: bulk-copy pipeline */
 } pic_config;
 
 typedef struct pic_handle pic_handle;
@@ -276,6 +277,25 @@ pic_status pic_run_host(pic_handle *h, long long n, const double *x, const doubl
                         const double *vx, const double *vy, long long nsteps, int prime,
                         double *x_out, double *y_out, double *vx_out, double *vy_out);
 
+/* ---- autotuning ---- */
+typedef struct pic_tune_result {
+    int chunk;            /* particles per push block                        */
+    int tile_w, tile_h;   /* sort tile (cells)                               */
+    int sort_every;       /* steps between counting sorts                    */
+    double ms_per_step;   /* measured with the chosen values                 */
+    int tried;            /* candidates timed                                */
+} pic_tune_result;
+/* Pick the push chunk (and with it the sort tile) and the sort cadence for a
+ * workload by timing short runs: for each candidate a handle is created from
+ * *cfg, species `species` is loaded from *spec, the leapfrog primed and
+ * `trial_steps` steps (rounded up to whole sort periods) timed with CUDA
+ * events after one warm-up period.  Chunk is searched first (4096, 8192,
+ * 16384) at the configured cadence, then the cadence (10, 20, 40, 80).  The
+ * chosen values are written into *cfg.  Needs the memory of one handle at a
+ * time. */
+pic_status pic_autotune(pic_config *cfg, int species, const pic_init_spec *spec,
+                        int trial_steps, pic_tune_result *out);
+
 /* ---- diagnostics ---- */
 typedef struct pic_diag {
     long long step;              /* completed steps                           */
@@ -291,7 +311,8 @@ typedef struct pic_diag {
 enum pic_device_errors {
     PIC_DEVERR_NAN = 1,       /* a particle had a non-finite velocity          */
     PIC_DEVERR_CAPACITY = 2,  /* a species ran out of capacity (ionisation)    */
-    PIC_DEVERR_CELL = 4       /* a cell index outside the grid was seen        */
+    PIC_DEVERR_CELL = 4,      /* a cell index outside the grid was seen        */
+    PIC_DEVERR_TIMEOUT = 8    /* a bounded device wait gave up                 */
 };
 
 pic_status pic_diagnostics(pic_handle *h, pic_diag *d);

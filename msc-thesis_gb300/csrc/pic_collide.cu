@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(256) mcc_kernel(MccArgs A)
     atomicAdd(&s_cnt[2], (unsigned long long)c_ion);
     atomicAdd(&s_cnt[3], (unsigned long long)c_null);
     const int any_over = __syncthreads_or(overflow ? 1 : 0);
-    if (threadIdx.x < 4) atomicAdd(&A.dev->coll[threadIdx.x], s_cnt[threadIdx.x]);
+    if (threadIdx.x < 4) atomicAdd(&A.dev->coll[threadIdx.x][acc_slot()], s_cnt[threadIdx.x]);
     if (threadIdx.x == 0 && any_over) atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_CAPACITY);
 }
 
@@ -272,8 +272,8 @@ __global__ void __launch_bounds__(256) ntc_kernel(NtcArgs A)
     atomicAdd(&s_cnt[1], (unsigned long long)ncand);
     __syncthreads();
     if (threadIdx.x == 0) {
-        atomicAdd(&A.dev->coll[4], s_cnt[0]);
-        atomicAdd(&A.dev->coll[5], s_cnt[1]);
+        atomicAdd(&A.dev->coll[4][acc_slot()], s_cnt[0]);
+        atomicAdd(&A.dev->coll[5][acc_slot()], s_cnt[1]);
     }
 }
 

@@ -28,27 +28,37 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
-// rho = (rho_fix - mean) * scale, rho_fix <- 0, sum(rho_fix) -> dev->q.
-// The background is removed in exact integer arithmetic before the single
-// rounding to float, so small perturbations of a large mean keep their
-// relative precision.
+__device__ __forceinline__ float fixed_to_float(unsigned long long v, long long mean_fix, float scale)
+{
+    // int64 -> float as hi * 2^32 + lo: two 32-bit conversions and one fma
+    // (at most one extra rounding)
+    const long long d = (long long)v - mean_fix;
+    return fmaf((float)(int)(d >> 32), 4294967296.0f, (float)(unsigned)(d & 0xFFFFFFFFll)) * scale;
+}
+
+// rho = (rho_fix - mean) * scale, sum(rho_fix) -> dev->q; rho_fix is cleared
+// by a memset after this kernel.  The background is removed in exact integer
+// arithmetic before the single rounding to float, so small perturbations of a
+// large mean keep their relative precision.  Two cells per thread per
+// iteration (16-byte loads, 8-byte stores; n is even).
 __global__ void __launch_bounds__(256)
-convert_kernel(unsigned long long *__restrict__ rho_fix, float *__restrict__ rho, long long n,
+convert_kernel(const unsigned long long *__restrict__ rho_fix, float *__restrict__ rho, long long n,
                long long mean_fix, float scale, DevState *dev)
 {
     __shared__ unsigned long long s_part[8];
     unsigned long long qs = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const unsigned long long v = rho_fix[i];
-        rho_fix[i] = 0ull;
+    const long long n2 = n >> 1;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
+        const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(rho_fix)[i];
+        qs += v.x + v.y;
+        reinterpret_cast<float2 *>(rho)[i] =
+            make_float2(fixed_to_float(v.x, mean_fix, scale), fixed_to_float(v.y, mean_fix, scale));
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long v = rho_fix[n - 1];
         qs += v;
-        // int64 -> float as hi * 2^32 + lo: two fast 32-bit conversions and
-        // one fma (at most one extra rounding) instead of the slow 64-bit
-        // conversion
-        const long long d = (long long)v - mean_fix;
-        const float f = fmaf((float)(int)(d >> 32), 4294967296.0f, (float)(unsigned)(d & 0xFFFFFFFFll));
-        rho[i] = f * scale;
+        rho[n - 1] = fixed_to_float(v, mean_fix, scale);
     }
     qs = warp_sum_u64(qs);
     if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = qs;
@@ -56,7 +66,7 @@ convert_kernel(unsigned long long *__restrict__ rho_fix, float *__restrict__ rho
     if (threadIdx.x == 0) {
         unsigned long long t = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_part[w];
-        atomicAdd(&dev->q, t);
+        atomicAdd(&dev->q[acc_slot()], t);
     }
 }
 
@@ -111,31 +121,39 @@ __global__ void __launch_bounds__(256) kspace_kernel(KspaceArgs A)
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_part[w];
-        atomicAdd(&A.dev->fe, t);
+        atomicAdd(&A.dev->fe[acc_slot()], t);
     }
 }
 
 // Moves the accumulators of the finished stage into the history ring and
-// clears them.  ADV_PUSH closes the particle pass of step s (kinetic energy
-// and momentum belong to step s) and advances the step counter; ADV_FIELD
-// records the field of the current step.
+// clears them; one warp, lane l folds slot l.  ADV_PUSH closes the particle
+// pass of step s (kinetic energy and momentum belong to step s) and advances
+// the step counter; ADV_FIELD records the field of the current step.
 __global__ void advance_kernel(DevState *d, double *hist, int cap, int kind, double fe_scale)
 {
+    const int l = threadIdx.x;  // 32 threads = ACC_SLOTS
     const long long s = d->step;
     const int k = (int)(s % cap);
     if (kind == ADV_PUSH) {
-        hist[1 * (size_t)cap + k] = d->ke;
-        hist[2 * (size_t)cap + k] = d->px;
-        hist[3 * (size_t)cap + k] = d->py;
-        d->ke = d->px = d->py = 0.0;
-        d->step = s + 1;
+        const double ke = warp_sum_d(d->ke[l]), px = warp_sum_d(d->px[l]), py = warp_sum_d(d->py[l]);
+        d->ke[l] = d->px[l] = d->py[l] = 0.0;
+        if (l == 0) {
+            hist[1 * (size_t)cap + k] = ke;
+            hist[2 * (size_t)cap + k] = px;
+            hist[3 * (size_t)cap + k] = py;
+            d->step = s + 1;
+        }
     } else {
-        hist[0 * (size_t)cap + k] = d->fe * fe_scale;
-        hist[4 * (size_t)cap + k] = (double)(long long)d->q;
-        hist[5 * (size_t)cap + k] = d->mode_amp;
-        d->fe = 0.0;
-        d->q = 0ull;
-        d->mode_amp = 0.0;
+        const double fe = warp_sum_d(d->fe[l]);
+        const unsigned long long q = warp_sum_u64(d->q[l]);
+        d->fe[l] = 0.0;
+        d->q[l] = 0ull;
+        if (l == 0) {
+            hist[0 * (size_t)cap + k] = fe * fe_scale;
+            hist[4 * (size_t)cap + k] = (double)(long long)q;
+            hist[5 * (size_t)cap + k] = d->mode_amp;
+            d->mode_amp = 0.0;
+        }
     }
 }
 
@@ -144,9 +162,10 @@ pic_status launch_convert(pic_handle *h)
     const Geometry &g = h->g;
     const long long n = (long long)g.nx * g.ny;
     const float scale = (float)(h->q_unit / (4294967296.0 * g.dx * g.dy));
-    convert_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(h->rho_fix, h->rho, n, h->mean_fix,
-                                                          scale, h->dev);
+    convert_kernel<<<grid_for((n + 1) / 2, 256), 256, 0, h->stream>>>(h->rho_fix, h->rho, n,
+                                                                    h->mean_fix, scale, h->dev);
     PIC_CUDA(cudaGetLastError());
+    PIC_CUDA(cudaMemsetAsync(h->rho_fix, 0, sizeof(unsigned long long) * (size_t)n, h->stream));
     return PIC_OK;
 }
 
@@ -177,7 +196,7 @@ pic_status launch_advance(pic_handle *h, int kind)
     const Geometry &g = h->g;
     // sum_n |E_n|^2 = N sum_k |E'^_k|^2 with E' the 1/N-scaled spectrum
     const double fe_scale = 0.5 * h->cfg.eps0 * g.dx * g.dy * (double)g.nx * (double)g.ny;
-    advance_kernel<<<1, 1, 0, h->stream>>>(h->dev, h->hist, h->hist_cap, kind, fe_scale);
+    advance_kernel<<<1, ACC_SLOTS, 0, h->stream>>>(h->dev, h->hist, h->hist_cap, kind, fe_scale);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }

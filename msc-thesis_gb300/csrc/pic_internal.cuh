@@ -95,19 +95,24 @@ struct SpeciesBuf {
 };
 
 // Device-side accumulators and counters (one struct in device memory).
+// Block-level partial sums go to one of ACC_SLOTS copies (block index mod
+// ACC_SLOTS) so that the blocks of a kernel, which finish together, do not
+// serialise on one address; the advance kernel folds the slots.
+constexpr int ACC_SLOTS = 32;
 struct DevState {
-    double ke, px, py;        // accumulated by the push of the current step
-    double fe;                // accumulated by the k-space kernel
+    double ke[ACC_SLOTS], px[ACC_SLOTS], py[ACC_SLOTS];  // push of the current step
+    double fe[ACC_SLOTS];                               // k-space kernel
+    unsigned long long q[ACC_SLOTS];                    // convert kernel (fixed-point charge)
+    unsigned long long coll[6][ACC_SLOTS];  // elastic, excitation, ionisation, null, DSMC collisions, pairs
     double mode_amp;          // |rho^| of the tracked mode
-    unsigned long long q;     // sum of the fixed-point density (convert kernel)
     long long step;           // completed steps
     long long n[PIC_MAX_SPECIES];
     unsigned int err;         // PIC_DEVERR_* bits
     unsigned int pad;
-    unsigned long long coll[6];  // elastic, excitation, ionisation, null, DSMC collisions, pairs
     unsigned long long mcc_pass, dsmc_pass;  // collision pass counters (Philox counters)
     long long mcc_n0;         // electron count at the start of the current MCC pass
 };
+__device__ __forceinline__ int acc_slot() { return (int)(blockIdx.x & (ACC_SLOTS - 1)); }
 
 // MCC configuration resolved for the device
 struct MccState {
@@ -173,6 +178,8 @@ struct pic_handle {
     // collision operators
     pic::MccState mcc;
     pic::DsmcState dsmc;
+    // push kernel variant: bulk-copy pipeline (chunk a multiple of its stage)
+    bool use_bulk = false;
 };
 
 namespace pic {
@@ -180,6 +187,7 @@ namespace pic {
 // ------------------------------------------------------------------ launchers
 // pic_push.cu
 pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale);
+size_t push_bulk_smem(const Geometry &g);
 pic_status launch_deposit(pic_handle *h, int s);
 // pic_field.cu
 pic_status launch_convert(pic_handle *h);

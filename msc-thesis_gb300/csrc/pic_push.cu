@@ -88,175 +88,189 @@ struct PushArgs {
     double ke_scale, p_scale; // m/4, m/2 (0 disables the diagnostics)
 };
 
-template <bool GATHER, bool DEPOSIT>
-__global__ void __launch_bounds__(256) push_kernel(PushArgs A)
+// Shared-memory window of a push block: E (float2) and the split deposit
+// accumulators, anchored at the tile of the block's first particle.
+struct Window {
+    float2 *sE;
+    unsigned *sLo, *sHi;
+    int wx0, wy0, nwx, nw;
+    bool on;
+};
+
+__device__ __forceinline__ Window setup_window(const PushArgs &A, unsigned char *smem, int anc)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const long long n = *A.d_n;
-    const long long base = (long long)blockIdx.x * A.chunk;
-    if (base >= n) return;  // block-uniform
-    const long long n4 = (n + 3) & ~3ll;
-    const long long end = min(base + (long long)A.chunk, n4);
+    Window W;
+    W.nwx = A.wcx + 1;
+    W.nw = W.nwx * (A.wcy + 1);
+    W.sE = reinterpret_cast<float2 *>(smem);
+    W.sLo = reinterpret_cast<unsigned *>(smem + (size_t)W.nw * sizeof(float2));
+    W.sHi = W.sLo + W.nw;
+    W.on = anc >= 0;
+    W.wx0 = W.wy0 = 0;
+    if (W.on) {
+        int wx0 = (anc & 0xFFFF) * A.tw - A.halo, wy0 = (anc >> 16) * A.th - A.halo;
+        wx0 %= A.nx;
+        if (wx0 < 0) wx0 += A.nx;
+        wy0 %= A.ny;
+        if (wy0 < 0) wy0 += A.ny;
+        W.wx0 = wx0;
+        W.wy0 = wy0;
+    }
+    return W;
+}
+
+template <bool GATHER, bool DEPOSIT>
+__device__ __forceinline__ void load_window(const PushArgs &A, const Window &W)
+{
+    if (!W.on) return;
+    for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
+        const int a = i % W.nwx, b = i / W.nwx;
+        const int gx = (W.wx0 + a) % A.nx, gy = (W.wy0 + b) % A.ny;
+        if (GATHER) W.sE[i] = make_float2(A.ex[(size_t)gy * A.nx + gx], A.ey[(size_t)gy * A.nx + gx]);
+        if (DEPOSIT) {
+            W.sLo[i] = 0u;
+            W.sHi[i] = 0u;
+        }
+    }
+}
+
+// one group of particles in one cell: window or global
+__device__ __forceinline__ void deposit_group(const PushArgs &A, const Window &W, int cx, int cy,
+                                              const Cic4 &C)
+{
+    int dxl = cx - W.wx0, dyl = cy - W.wy0;
+    if (dxl < 0) dxl += A.nx;
+    if (dyl < 0) dyl += A.ny;
+    if (W.on && dxl < A.wcx && dyl < A.wcy) {
+        const int i = dyl * W.nwx + dxl;
+        smem_add(W.sLo, W.sHi, i, C.w00);
+        smem_add(W.sLo, W.sHi, i + 1, C.w10);
+        smem_add(W.sLo, W.sHi, i + W.nwx, C.w01);
+        smem_add(W.sLo, W.sHi, i + W.nwx + 1, C.w11);
+    } else {
+        deposit_global(A.rho, A.nx, A.ny, cx, cy, C, A.qmul);
+    }
+}
+
+// Gather, push and deposit four consecutive particles held in registers.
+template <bool GATHER, bool DEPOSIT>
+__device__ __forceinline__ void push_quad(const PushArgs &A, const Window &W, int (&cc)[4],
+                                          float (&xo)[4], float (&yo)[4], float (&xv)[4],
+                                          float (&yv)[4], float &ke, float &px, float &py,
+                                          bool &bad)
+{
     const int nx = A.nx, ny = A.ny;
-
-    const int nwx = A.wcx + 1, nwy = A.wcy + 1, nw = nwx * nwy;
-    float2 *sE = reinterpret_cast<float2 *>(smem);
-    unsigned *sLo = reinterpret_cast<unsigned *>(smem + (size_t)nw * sizeof(float2));
-    unsigned *sHi = sLo + nw;
-    double *sAcc = reinterpret_cast<double *>(smem + (size_t)nw * 16);
-
-    const int anc = A.anchor[blockIdx.x];
-    const bool win = anc >= 0;
-    int wx0 = 0, wy0 = 0;
-    if (win) {
-        wx0 = (anc & 0xFFFF) * A.tw - A.halo;
-        wy0 = (anc >> 16) * A.th - A.halo;
-        wx0 %= nx;
-        if (wx0 < 0) wx0 += nx;
-        wy0 %= ny;
-        if (wy0 < 0) wy0 += ny;
-        for (int i = threadIdx.x; i < nw; i += blockDim.x) {
-            const int a = i % nwx, b = i / nwx;
-            const int gx = (wx0 + a) % nx, gy = (wy0 + b) % ny;
-            if (GATHER) sE[i] = make_float2(A.ex[(size_t)gy * nx + gx], A.ey[(size_t)gy * nx + gx]);
-            if (DEPOSIT) {
-                sLo[i] = 0u;
-                sHi[i] = 0u;
-            }
-        }
-    }
-    if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
-    __syncthreads();
-
-    // deposit of one group of particles in one cell: window or global
-    auto deposit = [&](int cx, int cy, const Cic4 &W) {
-        int dxl = cx - wx0, dyl = cy - wy0;
-        if (dxl < 0) dxl += nx;
-        if (dyl < 0) dyl += ny;
-        if (win && dxl < A.wcx && dyl < A.wcy) {
-            const int i = dyl * nwx + dxl;
-            smem_add(sLo, sHi, i, W.w00);
-            smem_add(sLo, sHi, i + 1, W.w10);
-            smem_add(sLo, sHi, i + nwx, W.w01);
-            smem_add(sLo, sHi, i + nwx + 1, W.w11);
-        } else {
-            deposit_global(A.rho, nx, ny, cx, cy, W, A.qmul);
-        }
-    };
-
-    float ke = 0.f, px = 0.f, py = 0.f;
-    bool bad = false;
-    for (long long q = base + 4ll * threadIdx.x; q < end; q += 4ll * blockDim.x) {
-        // plain (coherent) loads: with an in-place pass the same addresses are stored below
-        const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
-        const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
-        const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
-        const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
-        const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
-        int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-        float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
-        float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
-        // register aggregate of the particles that share the first one's new cell
-        unsigned gcnt = 0u, gfx = 0u, gfy = 0u;
-        unsigned long long gxy = 0ull;
-        int gkey = -1, gcx = 0, gcy = 0;
+    // register aggregate of the particles that share the first one's new cell
+    unsigned gcnt = 0u, gfx = 0u, gfy = 0u;
+    unsigned long long gxy = 0ull;
+    int gkey = -1, gcx = 0, gcy = 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int c = cc[j];
-            if (c < 0) continue;  // empty slot
-            int cx = c & 0xFFFF, cy = c >> 16;
-            if (cx >= nx || cy >= ny) {  // corrupt cell: flag, leave untouched
-                bad = true;
-                atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_CELL);
-                continue;
-            }
-            float ox = xo[j], oy = yo[j], vx = xv[j], vy = yv[j];
-            if (GATHER) {
-                const float gx = 1.f - ox, gy = 1.f - oy;
-                float2 e00, e10, e01, e11;
-                int dxl = cx - wx0, dyl = cy - wy0;
-                if (dxl < 0) dxl += nx;
-                if (dyl < 0) dyl += ny;
-                if (win && dxl < A.wcx && dyl < A.wcy) {
-                    const int i = dyl * nwx + dxl;
-                    e00 = sE[i];
-                    e10 = sE[i + 1];
-                    e01 = sE[i + nwx];
-                    e11 = sE[i + nwx + 1];
-                } else {
-                    const int cx1 = (cx + 1 == nx) ? 0 : cx + 1;
-                    const int cy1 = (cy + 1 == ny) ? 0 : cy + 1;
-                    const size_t i00 = (size_t)cy * nx + cx, i10 = (size_t)cy * nx + cx1;
-                    const size_t i01 = (size_t)cy1 * nx + cx, i11 = (size_t)cy1 * nx + cx1;
-                    e00 = make_float2(A.ex[i00], A.ey[i00]);
-                    e10 = make_float2(A.ex[i10], A.ey[i10]);
-                    e01 = make_float2(A.ex[i01], A.ey[i01]);
-                    e11 = make_float2(A.ex[i11], A.ey[i11]);
-                }
-                const float Ex = gy * fmaf(gx, e00.x, ox * e10.x) + oy * fmaf(gx, e01.x, ox * e11.x);
-                const float Ey = gy * fmaf(gx, e00.y, ox * e10.y) + oy * fmaf(gx, e01.y, ox * e11.y);
-                const float vx0 = vx, vy0 = vy;
-                vx = fmaf(A.qm_dt, Ex, vx);
-                vy = fmaf(A.qm_dt, Ey, vy);
-                ke = fmaf(vx0, vx0, fmaf(vy0, vy0, fmaf(vx, vx, fmaf(vy, vy, ke))));
-                px += vx0 + vx;
-                py += vy0 + vy;
+    for (int j = 0; j < 4; ++j) {
+        const int c = cc[j];
+        if (c < 0) continue;  // empty slot
+        int cx = c & 0xFFFF, cy = c >> 16;
+        if (cx >= nx || cy >= ny) {  // corrupt cell: flag, leave untouched
+            bad = true;
+            atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_CELL);
+            continue;
+        }
+        float ox = xo[j], oy = yo[j], vx = xv[j], vy = yv[j];
+        if (GATHER) {
+            const float gx = 1.f - ox, gy = 1.f - oy;
+            float2 e00, e10, e01, e11;
+            int dxl = cx - W.wx0, dyl = cy - W.wy0;
+            if (dxl < 0) dxl += nx;
+            if (dyl < 0) dyl += ny;
+            if (W.on && dxl < A.wcx && dyl < A.wcy) {
+                const int i = dyl * W.nwx + dxl;
+                e00 = W.sE[i];
+                e10 = W.sE[i + 1];
+                e01 = W.sE[i + W.nwx];
+                e11 = W.sE[i + W.nwx + 1];
             } else {
-                ke = fmaf(2.f * vx, vx, fmaf(2.f * vy, vy, ke));
-                px = fmaf(2.f, vx, px);
-                py = fmaf(2.f, vy, py);
+                const int cx1 = (cx + 1 == nx) ? 0 : cx + 1;
+                const int cy1 = (cy + 1 == ny) ? 0 : cy + 1;
+                const size_t i00 = (size_t)cy * nx + cx, i10 = (size_t)cy * nx + cx1;
+                const size_t i01 = (size_t)cy1 * nx + cx, i11 = (size_t)cy1 * nx + cx1;
+                e00 = make_float2(A.ex[i00], A.ey[i00]);
+                e10 = make_float2(A.ex[i10], A.ey[i10]);
+                e01 = make_float2(A.ex[i01], A.ey[i01]);
+                e11 = make_float2(A.ex[i11], A.ey[i11]);
             }
-            bad |= !(fabsf(vx) <= 3.0e38f) || !(fabsf(vy) <= 3.0e38f);
-            // drift in cell units; carry whole cells into the index
-            ox = fmaf(vx, A.dtdx, ox);
-            oy = fmaf(vy, A.dtdy, oy);
-            float sx = floorf(ox), sy = floorf(oy);
-            ox -= sx;
-            oy -= sy;
-            if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
-            if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
-            cx += (int)sx;
-            cy += (int)sy;
-            if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
-            if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
-            const int cn = cx | (cy << 16);
-            cc[j] = cn;
-            xo[j] = ox;
-            yo[j] = oy;
-            xv[j] = vx;
-            yv[j] = vy;
-            if (DEPOSIT) {
-                const unsigned fx = __float2uint_rn(ox * 65536.0f);
-                const unsigned fy = __float2uint_rn(oy * 65536.0f);
-                const unsigned long long fxy = (unsigned long long)fx * fy;
-                if (gkey < 0) {
-                    gkey = cn;
-                    gcx = cx;
-                    gcy = cy;
-                }
-                if (cn == gkey) {
-                    ++gcnt;
-                    gfx += fx;
-                    gfy += fy;
-                    gxy += fxy;
-                } else {
-                    deposit(cx, cy, cic_weights(1u, fx, fy, fxy));
-                }
+            const float Ex = gy * fmaf(gx, e00.x, ox * e10.x) + oy * fmaf(gx, e01.x, ox * e11.x);
+            const float Ey = gy * fmaf(gx, e00.y, ox * e10.y) + oy * fmaf(gx, e01.y, ox * e11.y);
+            const float vx0 = vx, vy0 = vy;
+            vx = fmaf(A.qm_dt, Ex, vx);
+            vy = fmaf(A.qm_dt, Ey, vy);
+            ke = fmaf(vx0, vx0, fmaf(vy0, vy0, fmaf(vx, vx, fmaf(vy, vy, ke))));
+            px += vx0 + vx;
+            py += vy0 + vy;
+        } else {
+            ke = fmaf(2.f * vx, vx, fmaf(2.f * vy, vy, ke));
+            px = fmaf(2.f, vx, px);
+            py = fmaf(2.f, vy, py);
+        }
+        bad |= !(fabsf(vx) <= 3.0e38f) || !(fabsf(vy) <= 3.0e38f);
+        // drift in cell units; carry whole cells into the index
+        ox = fmaf(vx, A.dtdx, ox);
+        oy = fmaf(vy, A.dtdy, oy);
+        float sx = floorf(ox), sy = floorf(oy);
+        ox -= sx;
+        oy -= sy;
+        if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
+        if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
+        cx += (int)sx;
+        cy += (int)sy;
+        if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
+        if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
+        const int cn = cx | (cy << 16);
+        cc[j] = cn;
+        xo[j] = ox;
+        yo[j] = oy;
+        xv[j] = vx;
+        yv[j] = vy;
+        if (DEPOSIT) {
+            const unsigned fx = __float2uint_rn(ox * 65536.0f);
+            const unsigned fy = __float2uint_rn(oy * 65536.0f);
+            const unsigned long long fxy = (unsigned long long)fx * fy;
+            if (gkey < 0) {
+                gkey = cn;
+                gcx = cx;
+                gcy = cy;
+            }
+            if (cn == gkey) {
+                ++gcnt;
+                gfx += fx;
+                gfy += fy;
+                gxy += fxy;
+            } else {
+                deposit_group(A, W, cx, cy, cic_weights(1u, fx, fy, fxy));
             }
         }
-        if (DEPOSIT && gcnt) deposit(gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
-        *reinterpret_cast<int4 *>(A.cout + q) = make_int4(cc[0], cc[1], cc[2], cc[3]);
-        *reinterpret_cast<float4 *>(A.oxout + q) = make_float4(xo[0], xo[1], xo[2], xo[3]);
-        *reinterpret_cast<float4 *>(A.oyout + q) = make_float4(yo[0], yo[1], yo[2], yo[3]);
-        *reinterpret_cast<float4 *>(A.vxout + q) = make_float4(xv[0], xv[1], xv[2], xv[3]);
-        *reinterpret_cast<float4 *>(A.vyout + q) = make_float4(yv[0], yv[1], yv[2], yv[3]);
-        if (A.pidin)
-            *reinterpret_cast<uint4 *>(A.pidout + q) = *reinterpret_cast<const uint4 *>(A.pidin + q);
-        if (A.vzin)
-            *reinterpret_cast<float4 *>(A.vzout + q) = *reinterpret_cast<const float4 *>(A.vzin + q);
     }
+    if (DEPOSIT && gcnt) deposit_group(A, W, gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+}
 
-    // diagnostics: FP32 per thread and per warp, FP64 across warps and blocks
+__device__ __forceinline__ void store_quad(const PushArgs &A, long long q, const int (&cc)[4],
+                                           const float (&xo)[4], const float (&yo)[4],
+                                           const float (&xv)[4], const float (&yv)[4])
+{
+    *reinterpret_cast<int4 *>(A.cout + q) = make_int4(cc[0], cc[1], cc[2], cc[3]);
+    *reinterpret_cast<float4 *>(A.oxout + q) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+    *reinterpret_cast<float4 *>(A.oyout + q) = make_float4(yo[0], yo[1], yo[2], yo[3]);
+    *reinterpret_cast<float4 *>(A.vxout + q) = make_float4(xv[0], xv[1], xv[2], xv[3]);
+    *reinterpret_cast<float4 *>(A.vyout + q) = make_float4(yv[0], yv[1], yv[2], yv[3]);
+    if (A.pidin)
+        *reinterpret_cast<uint4 *>(A.pidout + q) = *reinterpret_cast<const uint4 *>(A.pidin + q);
+    if (A.vzin)
+        *reinterpret_cast<float4 *>(A.vzout + q) = *reinterpret_cast<const float4 *>(A.vzin + q);
+}
+
+// end of a block: diagnostics reduction, error flags, window flush
+template <bool DEPOSIT>
+__device__ __forceinline__ void finish_block(const PushArgs &A, const Window &W, double *sAcc,
+                                             float ke, float px, float py, bool bad)
+{
     if (A.ke_scale != 0.0) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -273,22 +287,208 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
     const int any_bad = __syncthreads_or(bad ? 1 : 0);
     if (threadIdx.x == 0) {
         if (A.ke_scale != 0.0) {
-            atomicAdd(&A.dev->ke, sAcc[0] * A.ke_scale);
-            atomicAdd(&A.dev->px, sAcc[1] * A.p_scale);
-            atomicAdd(&A.dev->py, sAcc[2] * A.p_scale);
+            const int sl = acc_slot();
+            atomicAdd(&A.dev->ke[sl], sAcc[0] * A.ke_scale);
+            atomicAdd(&A.dev->px[sl], sAcc[1] * A.p_scale);
+            atomicAdd(&A.dev->py[sl], sAcc[2] * A.p_scale);
         }
         if (any_bad) atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_NAN);
     }
-    if (DEPOSIT && win) {
-        for (int i = threadIdx.x; i < nw; i += blockDim.x) {
-            const unsigned long long v = ((unsigned long long)sHi[i] << 16) + sLo[i];
+    if (DEPOSIT && W.on) {
+        for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
+            const unsigned long long v = ((unsigned long long)W.sHi[i] << 16) + W.sLo[i];
             if (v) {
-                const int a = i % nwx, b = i / nwx;
-                const int gx = (wx0 + a) % nx, gy = (wy0 + b) % ny;
-                atomicAdd(A.rho + (size_t)gy * nx + gx, v * A.qmul);
+                const int a = i % W.nwx, b = i / W.nwx;
+                const int gx = (W.wx0 + a) % A.nx, gy = (W.wy0 + b) % A.ny;
+                atomicAdd(A.rho + (size_t)gy * A.nx + gx, v * A.qmul);
             }
         }
     }
+}
+
+// Direct-load variant: each thread loads its quads with 128-bit loads.
+template <bool GATHER, bool DEPOSIT>
+__global__ void __launch_bounds__(256) push_kernel(PushArgs A)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const long long n = *A.d_n;
+    const long long base = (long long)blockIdx.x * A.chunk;
+    if (base >= n) return;  // block-uniform
+    const long long n4 = (n + 3) & ~3ll;
+    const long long end = min(base + (long long)A.chunk, n4);
+    const Window W = setup_window(A, smem, A.anchor[blockIdx.x]);
+    double *sAcc = reinterpret_cast<double *>(smem + (size_t)W.nw * 16);
+    load_window<GATHER, DEPOSIT>(A, W);
+    if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
+    __syncthreads();
+
+    float ke = 0.f, px = 0.f, py = 0.f;
+    bool bad = false;
+    for (long long q = base + 4ll * threadIdx.x; q < end; q += 4ll * blockDim.x) {
+        // plain (coherent) loads: with an in-place pass the same addresses are stored below
+        const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
+        const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
+        const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
+        const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+        const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+        int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+        float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
+        float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
+        push_quad<GATHER, DEPOSIT>(A, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+        store_quad(A, q, cc, xo, yo, xv, yv);
+    }
+    finish_block<DEPOSIT>(A, W, sAcc, ke, px, py, bad);
+}
+
+// ------------------------------------------------------------------------
+// Bulk-copy variant.  Thread 0 streams the chunk into shared memory through
+// a ring of PIPE_STAGES stages of STAGE_PARTICLES particles (five
+// cp.async.bulk copies per stage, completion counted in bytes on the
+// stage's mbarrier); all threads consume the stage from shared memory and
+// store results straight to global memory.  Memory parallelism comes from
+// the stages in flight, not from the number of resident warps.  Every wait
+// is bounded: on expiry the block raises PIC_DEVERR_TIMEOUT, waits (bounded)
+// for the copies it issued and leaves.
+// ------------------------------------------------------------------------
+constexpr int STAGE_PARTICLES = 1024;
+constexpr int PIPE_STAGES = 3;
+constexpr unsigned WAIT_LIMIT = 1u << 20;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity)
+{
+    for (unsigned it = 0; it < WAIT_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// shared memory of the bulk-copy variant: the window, the diagnostics, the
+// stage barriers, then the stage ring (16-byte aligned)
+__host__ __device__ __forceinline__ size_t tma_ring_offset(int nw)
+{
+    return (((size_t)nw * 16 + 32 + PIPE_STAGES * 8) + 127) & ~(size_t)127;
+}
+
+template <bool GATHER, bool DEPOSIT>
+__global__ void __launch_bounds__(256) push_kernel_bulk(PushArgs A)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const long long n = *A.d_n;
+    const long long base = (long long)blockIdx.x * A.chunk;
+    if (base >= n) return;  // block-uniform
+    const long long n4 = (n + 3) & ~3ll;
+    const long long end = min(base + (long long)A.chunk, n4);
+    const Window W = setup_window(A, smem, A.anchor[blockIdx.x]);
+    double *sAcc = reinterpret_cast<double *>(smem + (size_t)W.nw * 16);
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + (size_t)W.nw * 16 + 32);
+    unsigned char *ring = smem + tma_ring_offset(W.nw);
+    const int nstages = (int)((end - base + STAGE_PARTICLES - 1) / STAGE_PARTICLES);
+    const size_t field_bytes = (size_t)STAGE_PARTICLES * 4;
+    const size_t stage_bytes = 5 * field_bytes;
+
+    auto issue = [&](int k) {  // thread 0 only
+        const long long s0 = base + (long long)k * STAGE_PARTICLES;
+        const unsigned cnt = (unsigned)min((long long)STAGE_PARTICLES, end - s0);  // multiple of 4
+        const unsigned bytes = cnt * 4u;
+        unsigned char *dst = ring + (size_t)(k % PIPE_STAGES) * stage_bytes;
+        unsigned long long *b = bar + (k % PIPE_STAGES);
+        mbar_expect_tx(b, 5u * bytes);
+        bulk_g2s(dst + 0 * field_bytes, A.cin + s0, bytes, b);
+        bulk_g2s(dst + 1 * field_bytes, A.oxin + s0, bytes, b);
+        bulk_g2s(dst + 2 * field_bytes, A.oyin + s0, bytes, b);
+        bulk_g2s(dst + 3 * field_bytes, A.vxin + s0, bytes, b);
+        bulk_g2s(dst + 4 * field_bytes, A.vyin + s0, bytes, b);
+    };
+
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < PIPE_STAGES; ++k) mbar_init(bar + k, 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    load_window<GATHER, DEPOSIT>(A, W);
+    if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < PIPE_STAGES && k < nstages; ++k) issue(k);
+
+    float ke = 0.f, px = 0.f, py = 0.f;
+    bool bad = false;
+    int k = 0;
+    bool timed_out = false;
+    for (; k < nstages; ++k) {
+        const bool ok = mbar_wait_bounded(bar + (k % PIPE_STAGES), (unsigned)((k / PIPE_STAGES) & 1));
+        if (__syncthreads_or(ok ? 0 : 1)) {  // block-uniform decision
+            timed_out = true;
+            break;
+        }
+        const unsigned char *st = ring + (size_t)(k % PIPE_STAGES) * stage_bytes;
+        const long long s0 = base + (long long)k * STAGE_PARTICLES;
+        const int cnt = (int)min((long long)STAGE_PARTICLES, end - s0);
+        for (int l = 4 * threadIdx.x; l < cnt; l += 4 * blockDim.x) {
+            const int4 c4 = *reinterpret_cast<const int4 *>(st + 0 * field_bytes + 4 * l);
+            const float4 a4 = *reinterpret_cast<const float4 *>(st + 1 * field_bytes + 4 * l);
+            const float4 b4 = *reinterpret_cast<const float4 *>(st + 2 * field_bytes + 4 * l);
+            const float4 u4 = *reinterpret_cast<const float4 *>(st + 3 * field_bytes + 4 * l);
+            const float4 v4 = *reinterpret_cast<const float4 *>(st + 4 * field_bytes + 4 * l);
+            int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+            float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
+            float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
+            push_quad<GATHER, DEPOSIT>(A, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+            store_quad(A, s0 + l, cc, xo, yo, xv, yv);
+        }
+        __syncthreads();  // every thread is done with this stage's buffer
+        if (threadIdx.x == 0 && k + PIPE_STAGES < nstages) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(k + PIPE_STAGES);
+        }
+    }
+    if (timed_out) {
+        // wait (bounded) for the copies still in flight into this block's
+        // shared memory, report, and leave without flushing partial results
+        if (threadIdx.x == 0) {
+            for (int j = k; j < nstages && j < k + PIPE_STAGES; ++j)
+                mbar_wait_bounded(bar + (j % PIPE_STAGES), (unsigned)((j / PIPE_STAGES) & 1));
+            atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_TIMEOUT);
+        }
+        return;
+    }
+    finish_block<DEPOSIT>(A, W, sAcc, ke, px, py, bad);
 }
 
 // Deposit-only pass (after a sort or an import, before the first step):
@@ -327,6 +527,23 @@ __global__ void fixed_to_double_kernel(const unsigned long long *__restrict__ sr
 static size_t push_smem(const Geometry &g)
 {
     return (size_t)(g.wcx + 1) * (g.wcy + 1) * 16 + 32;
+}
+
+size_t push_bulk_smem(const Geometry &g)
+{
+    const int nw = (g.wcx + 1) * (g.wcy + 1);
+    return tma_ring_offset(nw) + (size_t)PIPE_STAGES * 5 * STAGE_PARTICLES * 4;
+}
+
+template <bool G, bool D> static pic_status bulk_attr(size_t sm)
+{
+    static size_t set = 0;
+    if (sm > set) {
+        PIC_CUDA(cudaFuncSetAttribute(push_kernel_bulk<G, D>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        set = sm;
+    }
+    return PIC_OK;
 }
 
 pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale)
@@ -374,16 +591,33 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
     A.p_scale = 0.5 * D.m;
     const bool charged = D.q != 0.0;
     const bool dep = deposit && D.q_int != 0;
-    const size_t sm = push_smem(g);
     dim3 grid((unsigned)B.nchunks), block(256);
-    if (charged && dep)
-        push_kernel<true, true><<<grid, block, sm, h->stream>>>(A);
-    else if (charged)
-        push_kernel<true, false><<<grid, block, sm, h->stream>>>(A);
-    else if (dep)
-        push_kernel<false, true><<<grid, block, sm, h->stream>>>(A);
-    else
-        push_kernel<false, false><<<grid, block, sm, h->stream>>>(A);
+    if (h->use_bulk) {
+        const size_t sm = push_bulk_smem(g);
+        if (charged && dep) {
+            PIC_TRY((bulk_attr<true, true>(sm)));
+            push_kernel_bulk<true, true><<<grid, block, sm, h->stream>>>(A);
+        } else if (charged) {
+            PIC_TRY((bulk_attr<true, false>(sm)));
+            push_kernel_bulk<true, false><<<grid, block, sm, h->stream>>>(A);
+        } else if (dep) {
+            PIC_TRY((bulk_attr<false, true>(sm)));
+            push_kernel_bulk<false, true><<<grid, block, sm, h->stream>>>(A);
+        } else {
+            PIC_TRY((bulk_attr<false, false>(sm)));
+            push_kernel_bulk<false, false><<<grid, block, sm, h->stream>>>(A);
+        }
+    } else {
+        const size_t sm = push_smem(g);
+        if (charged && dep)
+            push_kernel<true, true><<<grid, block, sm, h->stream>>>(A);
+        else if (charged)
+            push_kernel<true, false><<<grid, block, sm, h->stream>>>(A);
+        else if (dep)
+            push_kernel<false, true><<<grid, block, sm, h->stream>>>(A);
+        else
+            push_kernel<false, false><<<grid, block, sm, h->stream>>>(A);
+    }
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }

@@ -60,7 +60,7 @@ class Config(C.Structure):
                 ("dt", C.c_double), ("eps0", C.c_double), ("nspecies", C.c_int),
                 ("species", SpeciesDesc * MAX_SPECIES), ("sort_every", C.c_int),
                 ("tile_w", C.c_int), ("tile_h", C.c_int), ("chunk", C.c_int), ("halo", C.c_int),
-                ("history", C.c_int), ("device", C.c_int)]
+                ("history", C.c_int), ("device", C.c_int), ("push_variant", C.c_int)]
 
 
 class InitSpec(C.Structure):
@@ -92,6 +92,11 @@ class MccParams(C.Structure):
 class DsmcParams(C.Structure):
     _fields_ = [("species", C.c_int), ("diameter", C.c_double), ("weight", C.c_double),
                 ("depth", C.c_double), ("sigma_g_max0", C.c_double), ("seed", C.c_ulonglong)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("chunk", C.c_int), ("tile_w", C.c_int), ("tile_h", C.c_int),
+                ("sort_every", C.c_int), ("ms_per_step", C.c_double), ("tried", C.c_int)]
 
 
 class ParticlesView(C.Structure):
@@ -131,6 +136,7 @@ SIGNATURES = {
     "pic_set_mcc": [_H, C.POINTER(MccParams)],
     "pic_set_dsmc": [_H, C.POINTER(DsmcParams)],
     "pic_collision_counts": [_H, _vp],
+    "pic_autotune": [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p],
     "pic_step": [_H, C.c_longlong],
     "pic_run_host": [_H, C.c_longlong, _vp, _vp, _vp, _vp, C.c_longlong, C.c_int,
                      _vp, _vp, _vp, _vp],
@@ -227,6 +233,15 @@ def deposit_grid_noalloc(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale, rho_
     device memory; enqueues on `stream` and returns (see include/pic.h)."""
     _check(load().pic_deposit_grid_noalloc(nx, ny, n, cell_ptr, ox_ptr, oy_ptr, q_int, scale,
                                            rho_ptr, stream), "pic_deposit_grid_noalloc")
+
+
+def autotune(cfg: Config, species: int, spec: InitSpec, trial_steps: int = 40) -> TuneResult:
+    """Time candidate push chunks and sort cadences on this workload; the
+    chosen values are written into cfg (see pic_autotune in include/pic.h)."""
+    r = TuneResult()
+    _check(load().pic_autotune(C.addressof(cfg), species, C.addressof(spec), trial_steps,
+                               C.addressof(r)), "pic_autotune")
+    return r
 
 
 # ------------------------------------------------------------ handle ----

@@ -114,3 +114,18 @@ def test_init_matches_restatement():
     vy = 0.2 * rad * np.sin(2 * np.pi * uf(r0[:, 3]))
     np.testing.assert_allclose(a["vx"], vx, atol=2e-6)
     np.testing.assert_allclose(a["vy"], vy, atol=2e-6)
+
+
+def test_autotune_picks_a_working_config():
+    nx = ny = 128
+    n = nx * ny * 32
+    cfg, q, m = normalized_electrons(nx, ny, 6.4, 6.4, n, 0.05)
+    spec = P.init_spec(n, vth=(0.05, 0.05, 0), seed=8)
+    r = P.autotune(cfg, 0, spec, trial_steps=20)
+    assert r.tried >= 4 and r.ms_per_step > 0
+    assert cfg.chunk in (4096, 8192, 16384) and cfg.sort_every in (10, 20, 40, 80)
+    assert nx % cfg.tile_w == 0 and ny % cfg.tile_h == 0
+    with P.Handle(cfg) as h:  # the tuned config runs
+        h.init_particles(0, spec)
+        h.step(5)
+        assert h.diagnostics().error_flags == 0
