@@ -277,6 +277,55 @@ pic_status pic_run_host(pic_handle *h, long long n, const double *x, const doubl
                         const double *vx, const double *vy, long long nsteps, int prime,
                         double *x_out, double *y_out, double *vx_out, double *vy_out);
 
+/* ---- checkpoints ----
+ * A state file holds the grid geometry, the step and collision-pass
+ * counters and every species' particles (cell, offsets, velocities, ids) in
+ * storage order: little-endian, magic "PICSTATE", version 1.  A
+ * collisionless run resumed from a file continues bit for bit as the
+ * uninterrupted run; collision operators continue their random streams
+ * (keyed by particle id and pass counter).  Collision settings are not in
+ * the file: set them on the loading handle.  No counterpart in the
+ * reference (it keeps no state between runs). */
+pic_status pic_save(pic_handle *h, const char *path);
+/* Load a state file into a handle created with the same nx, ny, Lx, Ly and
+ * species count (same flags and q_int), each species' capacity at least the
+ * saved count; the field is recomputed from the loaded positions.  The
+ * whole file is read and checked first (cells on the grid or -1, offsets in
+ * [0, 1), finite velocities, ids a permutation, no trailing bytes): a bad
+ * file returns PIC_ERR_INVALID_ARG and leaves the handle unchanged. */
+pic_status pic_load(pic_handle *h, const char *path);
+
+/* ---- adjoint of the collisionless step ----
+ * Gradients of J = final field energy (1/2 eps0 sum |E|^2 dA after nsteps)
+ * by the discrete adjoint of the GPU step, for a handle with one charged
+ * species (species 0) and no collision operator.  The map differentiated
+ * is: v(-1/2) = v0 - (q/m) E(x0) dt/2, then nsteps leapfrog steps.
+ * Backward: a_v += dt a_x; a_x += [dt (q/m) dF/dx]^T a_v, where the transpose
+ * is the local CIC-gradient term, the scatter of mu = dt (q/m) a_v to the
+ * grid (the adjoint of the gather), the k-space solve psi^ = i k.g^ /
+ * (eps0 k^2) (the Poisson-gradient operator transposed) and the CIC-gradient
+ * gather of psi (the adjoint of the deposit).  Checkpoints of (x, v) every
+ * `every` steps; each segment is recomputed forward into a ring of positions
+ * and fields and walked backwards.  The run does not re-sort particles.
+ * The initial state is spec's load (spec != NULL) or the particles already
+ * loaded and not yet primed, as pic_set_particles leaves them (spec ==
+ * NULL).  Gradient arrays are in particle-id order (may be NULL).  With
+ * spec, dJ/d(beam_v) and dJ/d(pert_amp) follow from the initial gradients
+ * and the load's derivatives (pert_amp: PIC_PERT_XDISP and
+ * PIC_PERT_DENSITY; 0 for the other kinds).  The 2^-16 quantisation of the
+ * deposit weights is not differentiated.  Device memory: 20 bytes per
+ * particle slot per checkpoint plus `every` x (12 bytes per slot + 8 bytes
+ * per cell) for the ring.  Leaves the handle at step nsteps, with the
+ * history of the forward run.  No counterpart in the reference. */
+typedef struct pic_adjoint_result {
+    double J;           /* final field energy                                 */
+    double dJ_dbeam_v;  /* d J / d(spec->beam_v)   (spec given)               */
+    double dJ_damp;     /* d J / d(spec->pert_amp) (spec given)               */
+} pic_adjoint_result;
+pic_status pic_adjoint_run(pic_handle *h, const pic_init_spec *spec, long long nsteps, int every,
+                           double *dJ_dx0, double *dJ_dy0, double *dJ_dvx0, double *dJ_dvy0,
+                           pic_adjoint_result *out);
+
 /* ---- autotuning ---- */
 typedef struct pic_tune_result {
     int chunk;            /* particles per push block                        */

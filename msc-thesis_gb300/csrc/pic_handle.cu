@@ -217,7 +217,7 @@ static void update_mean(pic_handle *h)
 }
 
 // ---------------------------------------------------------------- stages
-static pic_status record_poisson(pic_handle *h)
+pic_status record_poisson(pic_handle *h)
 {
     PIC_TRY(launch_convert(h));
     PIC_CUFFT(cufftExecR2C(h->plan_r2c, h->rho, (cufftComplex *)h->rhohat));
@@ -230,7 +230,7 @@ static pic_status record_poisson(pic_handle *h)
 // Particle pass of one step.  src = 1: every species was just sorted into
 // buffer 1.  A DSMC species is sorted every step and collides on its sorted
 // buffer before its push moves it back; MCC follows the push.
-static pic_status record_push_all(pic_handle *h, int src, bool deposit)
+pic_status record_push_all(pic_handle *h, int src, bool deposit)
 {
     for (int s = 0; s < h->cfg.nspecies; ++s) {
         if (!h->sp[s].cap) continue;
@@ -292,7 +292,7 @@ static pic_status sort_now(pic_handle *h)
     return PIC_OK;
 }
 
-static pic_status deposit_now(pic_handle *h)
+pic_status deposit_now(pic_handle *h)
 {
     PIC_CUDA(cudaMemsetAsync(h->rho_fix, 0, sizeof(unsigned long long) * (size_t)h->g.nx * h->g.ny,
                              h->stream));
@@ -302,7 +302,7 @@ static pic_status deposit_now(pic_handle *h)
 }
 
 // After particles change from the host: sort, deposit, solve.
-static pic_status refresh(pic_handle *h)
+pic_status refresh(pic_handle *h)
 {
     update_mean(h);
     PIC_TRY(sort_now(h));
@@ -379,7 +379,7 @@ static pic_status need_species(pic_handle *h, int s)
     return PIC_OK;
 }
 
-static pic_status ensure_stage(pic_handle *h, size_t bytes)
+pic_status ensure_stage(pic_handle *h, size_t bytes)
 {
     if (h->stage_bytes >= bytes) return PIC_OK;
     cudaFree(h->stage);
@@ -401,6 +401,36 @@ static pic_status set_count(pic_handle *h, int s, long long n)
     // slots past n up to the next multiple of 4 must read as empty
     PIC_TRY(launch_fill_padding(h, s, n, std::max(old4, n4)));
     PIC_CUDA(cudaStreamSynchronize(h->stream));
+    return PIC_OK;
+}
+
+// After a state file was loaded into buffer 0: counts, padding, counters,
+// then sort, deposit and solve (the field is a function of the positions).
+pic_status handle_reload(pic_handle *h, const long long *n, long long step,
+                         unsigned long long mcc_pass, unsigned long long dsmc_pass)
+{
+    for (int s = 0; s < h->cfg.nspecies; ++s)
+        if (h->sp[s].cap) PIC_TRY(set_count(h, s, n[s]));
+    PIC_TRY(reset_device_state(h));
+    PIC_CUDA(cudaMemcpy(&h->dev->step, &step, sizeof step, cudaMemcpyHostToDevice));
+    PIC_CUDA(cudaMemcpy(&h->dev->mcc_pass, &mcc_pass, sizeof mcc_pass, cudaMemcpyHostToDevice));
+    PIC_CUDA(cudaMemcpy(&h->dev->dsmc_pass, &dsmc_pass, sizeof dsmc_pass, cudaMemcpyHostToDevice));
+    h->steps_host = step;
+    return refresh(h);
+}
+
+pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly)
+{
+    const long long nc = (long long)h->g.nx * h->g.ny;
+    if (n % nc) {
+        set_error("lattice load needs a whole number of particles per cell");
+        return PIC_ERR_INVALID_ARG;
+    }
+    const long long ppc = n / nc;
+    long long a = (long long)std::ceil(std::sqrt((double)ppc));
+    while (ppc % a) ++a;  // smallest divisor >= sqrt(ppc): more sites along x
+    *lx = (int)(h->g.nx * a);
+    *ly = (int)(h->g.ny * (ppc / a));
     return PIC_OK;
 }
 
@@ -595,21 +625,6 @@ pic_status pic_synchronize(pic_handle *h)
     PIC_TRY(need(h));
     PIC_CUDA(cudaStreamSynchronize(h->stream));
     return check_flags(h);
-}
-
-static pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly)
-{
-    const long long nc = (long long)h->g.nx * h->g.ny;
-    if (n % nc) {
-        set_error("lattice load needs a whole number of particles per cell");
-        return PIC_ERR_INVALID_ARG;
-    }
-    const long long ppc = n / nc;
-    long long a = (long long)std::ceil(std::sqrt((double)ppc));
-    while (ppc % a) ++a;  // smallest divisor >= sqrt(ppc): more sites along x
-    *lx = (int)(h->g.nx * a);
-    *ly = (int)(h->g.ny * (ppc / a));
-    return PIC_OK;
 }
 
 pic_status pic_init_particles(pic_handle *h, int s, const pic_init_spec *spec)

@@ -208,6 +208,56 @@ pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_
     return PIC_OK;
 }
 
+// d(x, y)/d(pert_amp) of init_kernel's position, in id order.  XDISP:
+// (cos(kx x_lat), 0); DENSITY: -k sin(k.x_lat) / |k|^2; other kinds: 0.
+__global__ void init_damp_kernel(InitArgs A, double *dxa, double *dya)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += stride) {
+        double x, y;
+        if (A.layout == PIC_LOAD_LATTICE) {
+            const long long ix = i % A.lat_nx, iy = i / A.lat_nx;
+            x = ((double)ix + 0.5) * (A.Lx / A.lat_nx);
+            y = ((double)iy + 0.5) * (A.Ly / A.lat_ny);
+        } else {
+            const U4 r0 = philox4x32_10(U4{(uint32_t)i, (uint32_t)(i >> 32), 0u, STREAM_INIT}, A.k0, A.k1);
+            x = u01d(r0.x) * A.Lx;
+            y = u01d(r0.y) * A.Ly;
+        }
+        double gx = 0.0, gy = 0.0;
+        if (A.pert_kind == PIC_PERT_XDISP) {
+            gx = cos(A.kx * x);
+        } else if (A.pert_kind == PIC_PERT_DENSITY) {
+            const double k2 = A.kx * A.kx + A.ky * A.ky;
+            const double s = sin(A.kx * x + A.ky * y) / k2;
+            gx = -A.kx * s;
+            gy = -A.ky * s;
+        }
+        dxa[i] = gx;
+        dya[i] = gy;
+    }
+}
+
+pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
+                          double *dxdA, double *dydA)
+{
+    InitArgs A = base_args(h, 0);
+    A.n = spec->n;
+    A.layout = spec->layout;
+    A.pert_kind = spec->pert_kind;
+    A.lat_nx = lat_nx;
+    A.lat_ny = lat_ny;
+    A.kx = 2.0 * 3.14159265358979323846 * spec->pert_mx / h->g.Lx;
+    A.ky = 2.0 * 3.14159265358979323846 * spec->pert_my / h->g.Ly;
+    A.k0 = (uint32_t)spec->seed;
+    A.k1 = (uint32_t)(spec->seed >> 32);
+    if (A.n > 0) {
+        init_damp_kernel<<<grid_for(A.n, 256), 256, 0, h->stream>>>(A, dxdA, dydA);
+        PIC_CUDA(cudaGetLastError());
+    }
+    return PIC_OK;
+}
+
 pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x_dev,
                               const double *y_dev, const double *vx_dev, const double *vy_dev,
                               const double *vz_dev)

@@ -207,8 +207,18 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
 pic_status launch_to_global(pic_handle *h, int s, double *x_dev, double *y_dev, double *vx_dev,
                             double *vy_dev, double *vz_dev);
 pic_status launch_fill_padding(pic_handle *h, int s, long long from, long long to);
+pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
+                          double *dxdA, double *dydA);
 
 // grid-stride launch size for `n` items on the current device
 int grid_for(long long n, int block);
+
+// pic_handle.cu stages used by other host files
+pic_status record_poisson(pic_handle *h);
+pic_status record_push_all(pic_handle *h, int src, bool deposit);
+pic_status deposit_now(pic_handle *h);
+pic_status refresh(pic_handle *h);
+pic_status ensure_stage(pic_handle *h, size_t bytes);
+pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly);
 
 }  // namespace pic

@@ -99,6 +99,10 @@ class TuneResult(C.Structure):
                 ("sort_every", C.c_int), ("ms_per_step", C.c_double), ("tried", C.c_int)]
 
 
+class AdjointResult(C.Structure):
+    _fields_ = [("J", C.c_double), ("dJ_dbeam_v", C.c_double), ("dJ_damp", C.c_double)]
+
+
 class ParticlesView(C.Structure):
     _fields_ = [("n", C.c_longlong), ("cell_dev", C.c_void_p), ("ox_dev", C.c_void_p),
                 ("oy_dev", C.c_void_p), ("vx_dev", C.c_void_p), ("vy_dev", C.c_void_p),
@@ -137,6 +141,10 @@ SIGNATURES = {
     "pic_set_dsmc": [_H, C.POINTER(DsmcParams)],
     "pic_collision_counts": [_H, _vp],
     "pic_autotune": [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p],
+    "pic_save": [_H, C.c_char_p],
+    "pic_load": [_H, C.c_char_p],
+    "pic_adjoint_run": [_H, _vp, C.c_longlong, C.c_int, _vp, _vp, _vp, _vp,
+                        C.POINTER(AdjointResult)],
     "pic_step": [_H, C.c_longlong],
     "pic_run_host": [_H, C.c_longlong, _vp, _vp, _vp, _vp, C.c_longlong, C.c_int,
                      _vp, _vp, _vp, _vp],
@@ -342,6 +350,11 @@ class Handle:
         self._keep = (x, y, vx, vy, vz)
         self._c("pic_set_particles", s, len(x), _ptr(x), _ptr(y), _ptr(vx), _ptr(vy), _ptr(vz))
 
+    def count(self, s=0) -> int:
+        n = C.c_longlong()
+        self._c("pic_get_particles", s, C.byref(n), None, None, None, None, None)
+        return n.value
+
     def get_particles(self, s=0, vz=False):
         n = C.c_longlong()
         self._c("pic_get_particles", s, C.byref(n), None, None, None, None, None)
@@ -404,6 +417,23 @@ class Handle:
         p = DsmcParams(species, diameter, weight, depth, sigma_g_max0, seed)
         self._c("pic_set_dsmc", C.byref(p))
 
+    def save(self, path):
+        self._c("pic_save", os.fsencode(path))
+
+    def load(self, path):
+        self._c("pic_load", os.fsencode(path))
+
+    def adjoint(self, nsteps, every=10, spec: InitSpec | None = None):
+        """Final field energy J and its gradients with respect to the initial
+        state (pic_adjoint_run).  Returns (AdjointResult, dJ/dx0, dJ/dy0,
+        dJ/dvx0, dJ/dvy0), arrays in particle-id order."""
+        n = spec.n if spec is not None else self.count(0)
+        out = [np.empty(n) for _ in range(4)]
+        r = AdjointResult()
+        self._c("pic_adjoint_run", C.addressof(spec) if spec is not None else None, int(nsteps),
+                int(every), *[_ptr(o) for o in out], C.byref(r))
+        return (r, *out)
+
     def collision_counts(self):
         c = np.zeros(6, dtype=np.int64)
         self._c("pic_collision_counts", _ptr(c))
@@ -448,3 +478,28 @@ class Handle:
         out = np.empty((self.cfg.ny, self.cfg.nx), np.int64)
         self._c("pic_get_rho_fixed", _ptr(out))
         return out
+
+
+def field_energy_function(handle: Handle, nsteps: int, every: int = 10):
+    """A torch.autograd.Function for J(x0, y0, vx0, vy0) = field energy after
+    `nsteps` steps of `handle`'s species 0 from that initial state (unprimed).
+    The forward pass runs pic_adjoint_run, so the gradients are computed with
+    J; backward scales them by the incoming gradient.  Inputs are 1-D tensors
+    of one length (any device, float64 recommended); they pass through host
+    memory."""
+    import torch
+
+    class _FieldEnergy(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x0, y0, vx0, vy0):
+            arrs = [t.detach().to("cpu", torch.float64).numpy() for t in (x0, y0, vx0, vy0)]
+            handle.set_particles(0, *arrs)
+            r, *grads = handle.adjoint(nsteps, every)
+            ctx.save_for_backward(*[torch.from_numpy(g).to(x0.device, x0.dtype) for g in grads])
+            return x0.new_tensor(r.J)
+
+        @staticmethod
+        def backward(ctx, gJ):
+            return tuple(gJ * g for g in ctx.saved_tensors)
+
+    return _FieldEnergy.apply

@@ -265,3 +265,28 @@ def dsmc_run(d: dict, x, y, vx, vy, vz, sgmax, nsteps, first_pass=0):
     L.orc_dsmc_run(C.byref(dc), len(x), _p(x), _p(y), _p(vx), _p(vy), _p(vz), _p(sg), nsteps,
                    first_pass, _p(te), _p(to), counts.ctypes.data)
     return dict(x=x, y=y, vx=vx, vy=vy, vz=vz, T_even=te, T_odd=to, counts=counts)
+
+
+# ---------------------------------------------------------------- adjoint ----
+def adjoint(cfg: PhysCfg, x0, y0, vx0, vy0, q, m, nsteps, nthreads=0):
+    """FP64 forward + adjoint (restatement): returns (J, dJ/dx0, dJ/dy0, dJ/dvx0, dJ/dvy0)."""
+    L = lib()
+    L.orc_adjoint.restype = C.c_double
+    L.orc_adjoint.argtypes = [C.POINTER(PhysCfg), C.c_long, C.c_double, C.c_double, _dp, _dp, _dp,
+                              _dp, C.c_long, _dp, _dp, _dp, _dp, C.c_int]
+    x0, y0, vx0, vy0 = (_f64(a) for a in (x0, y0, vx0, vy0))
+    n = len(x0)
+    out = [np.empty(n) for _ in range(4)]
+    J = L.orc_adjoint(C.byref(cfg), n, q, m, _p(x0), _p(y0), _p(vx0), _p(vy0), nsteps,
+                      *[_p(o) for o in out], nthreads)
+    return (J, *out)
+
+
+def forward_J(cfg: PhysCfg, x0, y0, vx0, vy0, q, m, nsteps, nthreads=0):
+    L = lib()
+    L.orc_forward_J.restype = C.c_double
+    L.orc_forward_J.argtypes = [C.POINTER(PhysCfg), C.c_long, C.c_double, C.c_double, _dp, _dp,
+                                _dp, _dp, C.c_long, C.c_int]
+    x0, y0, vx0, vy0 = (_f64(a) for a in (x0, y0, vx0, vy0))
+    return L.orc_forward_J(C.byref(cfg), len(x0), q, m, _p(x0), _p(y0), _p(vx0), _p(vy0), nsteps,
+                           nthreads)

@@ -861,3 +861,323 @@ void orc_dsmc_run(const orc_dsmc *d, long n, double *x, double *y, double *vx, d
     free(idx);
     free(cell);
 }
+
+/* ===================================================================== */
+/* Part 5: adjoint of the physics step (FP64).                           */
+/* ===================================================================== */
+typedef struct adj_ctx {
+    const orc_phys_cfg *c;
+    int nx, ny;
+    double dx, dy, dA;
+    long n;
+    double q, m;
+    int nthreads;
+} adj_ctx;
+
+/* E from positions: deposit (with background) + spectral solve */
+static void adj_fields(const adj_ctx *A, const double *x, const double *y, double *ex, double *ey)
+{
+    orc_species sp;
+    sp.n = A->n;
+    sp.q = A->q;
+    sp.m = A->m;
+    sp.x = (double *)x;
+    sp.y = (double *)y;
+    sp.vx = sp.vy = NULL;
+    orc_phys_cfg c1 = *A->c;
+    c1.nspecies = 1;
+    orc_phys_fields(&c1, &sp, NULL, NULL, ex, ey, A->nthreads);
+}
+
+typedef struct cicw {
+    int i00, i10, i01, i11;
+    double fx, fy;
+} cicw;
+
+static inline cicw adj_locate(const adj_ctx *A, double x, double y)
+{
+    cicw w;
+    int ix, iy;
+    cic_locate(x, A->dx, A->nx, &ix, &w.fx);
+    cic_locate(y, A->dy, A->ny, &iy, &w.fy);
+    int ix1 = (ix + 1) % A->nx, iy1 = (iy + 1) % A->ny;
+    w.i00 = iy * A->nx + ix;
+    w.i10 = iy * A->nx + ix1;
+    w.i01 = iy1 * A->nx + ix;
+    w.i11 = iy1 * A->nx + ix1;
+    return w;
+}
+
+/* F = sum_k w_k E_k for one particle */
+static inline void adj_gather(const cicw *w, const double *ex, const double *ey, double *Fx, double *Fy)
+{
+    double gx = 1.0 - w->fx, gy = 1.0 - w->fy;
+    *Fx = gx * gy * ex[w->i00] + w->fx * gy * ex[w->i10] + gx * w->fy * ex[w->i01] + w->fx * w->fy * ex[w->i11];
+    *Fy = gx * gy * ey[w->i00] + w->fx * gy * ey[w->i10] + gx * w->fy * ey[w->i01] + w->fx * w->fy * ey[w->i11];
+}
+
+/* sum_k grad w_k * s_k  (s scalar per node), in physical units */
+static inline void adj_grad_dot(const adj_ctx *A, const cicw *w, double s00, double s10, double s01,
+                                double s11, double *gx, double *gy)
+{
+    double fx = w->fx, fy = w->fy;
+    *gx = ((1.0 - fy) * (s10 - s00) + fy * (s11 - s01)) / A->dx;
+    *gy = ((1.0 - fx) * (s01 - s00) + fx * (s11 - s10)) / A->dy;
+}
+
+/* psi = S^T g  with S: rho -> E (spectral, Nyquist derivative zeroed) */
+static void adj_solve_T(const adj_ctx *A, const double *gxg, const double *gyg, double *psi)
+{
+    const int nx = A->nx, ny = A->ny, nh = nx / 2 + 1;
+    const size_t nk = (size_t)ny * nh, ng = (size_t)nx * ny;
+    double *ax = (double *)malloc(sizeof(double) * 2 * nk), *ay = (double *)malloc(sizeof(double) * 2 * nk);
+    double *ph = (double *)malloc(sizeof(double) * 2 * nk);
+    orc_fft2d_r2c(ny, nx, gxg, ax);
+    orc_fft2d_r2c(ny, nx, gyg, ay);
+    for (int my = 0; my < ny; ++my) {
+        int sy = (my <= ny / 2) ? my : my - ny;
+        double ky = 2.0 * M_PI * sy / A->c->Ly;
+        for (int mx = 0; mx < nh; ++mx) {
+            double kx = 2.0 * M_PI * mx / A->c->Lx;
+            size_t qq = (size_t)my * nh + mx;
+            double k2 = kx * kx + ky * ky;
+            double kxe = ((nx % 2 == 0) && mx == nx / 2) ? 0.0 : kx;
+            double kye = ((ny % 2 == 0) && my == ny / 2) ? 0.0 : ky;
+            double hr = kxe * ax[2 * qq] + kye * ay[2 * qq];
+            double hi = kxe * ax[2 * qq + 1] + kye * ay[2 * qq + 1];
+            double inv = (mx == 0 && my == 0) ? 0.0 : 1.0 / (A->c->eps0 * k2);
+            /* i (hr + i hi) = -hi + i hr */
+            ph[2 * qq] = -hi * inv;
+            ph[2 * qq + 1] = hr * inv;
+        }
+    }
+    orc_fft2d_c2r(ny, nx, ph, psi);
+    for (size_t i = 0; i < ng; ++i) psi[i] /= (double)ng;
+    free(ax);
+    free(ay);
+    free(ph);
+}
+
+/* a_x += (q/dA) sum_m psi_m grad w_m(x) for every particle */
+static void adj_gather_psi(const adj_ctx *A, const double *x, const double *y, const double *psi,
+                           double *axv, double *ayv)
+{
+    const double s = A->q / A->dA;
+#pragma omp parallel for num_threads(A->nthreads) schedule(static)
+    for (long i = 0; i < A->n; ++i) {
+        cicw w = adj_locate(A, x[i], y[i]);
+        double gx, gy;
+        adj_grad_dot(A, &w, psi[w.i00], psi[w.i10], psi[w.i01], psi[w.i11], &gx, &gy);
+        axv[i] += s * gx;
+        ayv[i] += s * gy;
+    }
+}
+
+/* kick adjoint with coefficient C (= dt q/m, or -dt/2 q/m for the priming) */
+static void adj_kick(const adj_ctx *A, const double *x, const double *y, const double *ex,
+                     const double *ey, const double *avx, const double *avy, double C, double *axv,
+                     double *ayv)
+{
+    const size_t ng = (size_t)A->nx * A->ny;
+    double *g = (double *)calloc(2 * ng, sizeof(double));
+    double *psi = (double *)malloc(sizeof(double) * ng);
+    for (long i = 0; i < A->n; ++i) {  /* serial scatter: deterministic */
+        cicw w = adj_locate(A, x[i], y[i]);
+        double mx = C * avx[i], my = C * avy[i];
+        double gx_ = 1.0 - w.fx, gy_ = 1.0 - w.fy;
+        double w00 = gx_ * gy_, w10 = w.fx * gy_, w01 = gx_ * w.fy, w11 = w.fx * w.fy;
+        g[w.i00] += w00 * mx; g[ng + w.i00] += w00 * my;
+        g[w.i10] += w10 * mx; g[ng + w.i10] += w10 * my;
+        g[w.i01] += w01 * mx; g[ng + w.i01] += w01 * my;
+        g[w.i11] += w11 * mx; g[ng + w.i11] += w11 * my;
+        /* local term: sum_k grad w_k (E_k . mu) */
+        double s00 = ex[w.i00] * mx + ey[w.i00] * my, s10 = ex[w.i10] * mx + ey[w.i10] * my;
+        double s01 = ex[w.i01] * mx + ey[w.i01] * my, s11 = ex[w.i11] * mx + ey[w.i11] * my;
+        double lx, ly;
+        adj_grad_dot(A, &w, s00, s10, s01, s11, &lx, &ly);
+        axv[i] += lx;
+        ayv[i] += ly;
+    }
+    adj_solve_T(A, g, g + ng, psi);
+    adj_gather_psi(A, x, y, psi, axv, ayv);
+    free(g);
+    free(psi);
+}
+
+static void adj_forward(const adj_ctx *A, const double *x0, const double *y0, const double *vx0,
+                        const double *vy0, long nsteps, double *X, double *Y, double *J)
+{
+    /* X, Y: (nsteps+1) * n positions; returns J */
+    const size_t ng = (size_t)A->nx * A->ny;
+    const long n = A->n;
+    const double dt = A->c->dt, qm = A->q / A->m;
+    double *vx = (double *)malloc(sizeof(double) * n), *vy = (double *)malloc(sizeof(double) * n);
+    double *ex = (double *)malloc(sizeof(double) * ng), *ey = (double *)malloc(sizeof(double) * ng);
+    memcpy(X, x0, sizeof(double) * n);
+    memcpy(Y, y0, sizeof(double) * n);
+    memcpy(vx, vx0, sizeof(double) * n);
+    memcpy(vy, vy0, sizeof(double) * n);
+    adj_fields(A, X, Y, ex, ey);
+    for (long i = 0; i < n; ++i) { /* priming: v(-1/2) = v0 - (q/m) F(x0) dt/2 */
+        cicw w = adj_locate(A, X[i], Y[i]);
+        double Fx, Fy;
+        adj_gather(&w, ex, ey, &Fx, &Fy);
+        vx[i] -= 0.5 * dt * qm * Fx;
+        vy[i] -= 0.5 * dt * qm * Fy;
+    }
+    for (long st = 0; st < nsteps; ++st) {
+        const double *xs = X + (size_t)st * n, *ys = Y + (size_t)st * n;
+        double *xn = X + (size_t)(st + 1) * n, *yn = Y + (size_t)(st + 1) * n;
+        if (st > 0) adj_fields(A, xs, ys, ex, ey);
+#pragma omp parallel for num_threads(A->nthreads) schedule(static)
+        for (long i = 0; i < n; ++i) {
+            cicw w = adj_locate(A, xs[i], ys[i]);
+            double Fx, Fy;
+            adj_gather(&w, ex, ey, &Fx, &Fy);
+            vx[i] += dt * qm * Fx;
+            vy[i] += dt * qm * Fy;
+            double x = xs[i] + dt * vx[i], y = ys[i] + dt * vy[i];
+            x -= A->c->Lx * floor(x / A->c->Lx);
+            y -= A->c->Ly * floor(y / A->c->Ly);
+            if (x >= A->c->Lx) x -= A->c->Lx;
+            if (y >= A->c->Ly) y -= A->c->Ly;
+            xn[i] = x;
+            yn[i] = y;
+        }
+    }
+    adj_fields(A, X + (size_t)nsteps * n, Y + (size_t)nsteps * n, ex, ey);
+    double fe = 0.0;
+    for (size_t i = 0; i < ng; ++i) fe += ex[i] * ex[i] + ey[i] * ey[i];
+    *J = 0.5 * A->c->eps0 * fe * A->dA;
+    free(vx);
+    free(vy);
+    free(ex);
+    free(ey);
+}
+
+static adj_ctx make_ctx(const orc_phys_cfg *c, long n, double q, double m, int nthreads)
+{
+    adj_ctx A;
+    A.c = c;
+    A.nx = c->nx;
+    A.ny = c->ny;
+    A.dx = c->Lx / c->nx;
+    A.dy = c->Ly / c->ny;
+    A.dA = A.dx * A.dy;
+    A.n = n;
+    A.q = q;
+    A.m = m;
+    A.nthreads = clamp_threads(nthreads);
+    return A;
+}
+
+double orc_forward_J(const orc_phys_cfg *c, long n, double q, double m, const double *x0,
+                     const double *y0, const double *vx0, const double *vy0, long nsteps,
+                     int nthreads)
+{
+    adj_ctx A = make_ctx(c, n, q, m, nthreads);
+    double *X = (double *)malloc(sizeof(double) * 2 * (size_t)n);
+    double *Y = (double *)malloc(sizeof(double) * 2 * (size_t)n);
+    /* forward without keeping the trajectory: reuse two position slots */
+    const size_t ng = (size_t)A.nx * A.ny;
+    const double dt = c->dt, qm = q / m;
+    double *vx = (double *)malloc(sizeof(double) * n), *vy = (double *)malloc(sizeof(double) * n);
+    double *ex = (double *)malloc(sizeof(double) * ng), *ey = (double *)malloc(sizeof(double) * ng);
+    memcpy(X, x0, sizeof(double) * n);
+    memcpy(Y, y0, sizeof(double) * n);
+    memcpy(vx, vx0, sizeof(double) * n);
+    memcpy(vy, vy0, sizeof(double) * n);
+    adj_fields(&A, X, Y, ex, ey);
+    for (long i = 0; i < n; ++i) {
+        cicw w = adj_locate(&A, X[i], Y[i]);
+        double Fx, Fy;
+        adj_gather(&w, ex, ey, &Fx, &Fy);
+        vx[i] -= 0.5 * dt * qm * Fx;
+        vy[i] -= 0.5 * dt * qm * Fy;
+    }
+    for (long st = 0; st < nsteps; ++st) {
+        if (st > 0) adj_fields(&A, X, Y, ex, ey);
+#pragma omp parallel for num_threads(A.nthreads) schedule(static)
+        for (long i = 0; i < n; ++i) {
+            cicw w = adj_locate(&A, X[i], Y[i]);
+            double Fx, Fy;
+            adj_gather(&w, ex, ey, &Fx, &Fy);
+            vx[i] += dt * qm * Fx;
+            vy[i] += dt * qm * Fy;
+            double x = X[i] + dt * vx[i], y = Y[i] + dt * vy[i];
+            x -= c->Lx * floor(x / c->Lx);
+            y -= c->Ly * floor(y / c->Ly);
+            if (x >= c->Lx) x -= c->Lx;
+            if (y >= c->Ly) y -= c->Ly;
+            X[i] = x;
+            Y[i] = y;
+        }
+    }
+    adj_fields(&A, X, Y, ex, ey);
+    double fe = 0.0;
+    for (size_t i = 0; i < ng; ++i) fe += ex[i] * ex[i] + ey[i] * ey[i];
+    free(X);
+    free(Y);
+    free(vx);
+    free(vy);
+    free(ex);
+    free(ey);
+    return 0.5 * c->eps0 * fe * A.dA;
+}
+
+double orc_adjoint(const orc_phys_cfg *c, long n, double q, double m, const double *x0,
+                   const double *y0, const double *vx0, const double *vy0, long nsteps,
+                   double *gx0, double *gy0, double *gvx0, double *gvy0, int nthreads)
+{
+    adj_ctx A = make_ctx(c, n, q, m, nthreads);
+    const size_t ng = (size_t)A.nx * A.ny;
+    double *X = (double *)malloc(sizeof(double) * (size_t)(nsteps + 1) * n);
+    double *Y = (double *)malloc(sizeof(double) * (size_t)(nsteps + 1) * n);
+    double J = 0.0;
+    adj_forward(&A, x0, y0, vx0, vy0, nsteps, X, Y, &J);
+    double *ax = (double *)calloc(n, sizeof(double)), *ay = (double *)calloc(n, sizeof(double));
+    double *avx = (double *)calloc(n, sizeof(double)), *avy = (double *)calloc(n, sizeof(double));
+    double *ex = (double *)malloc(sizeof(double) * ng), *ey = (double *)malloc(sizeof(double) * ng);
+    double *g = (double *)malloc(sizeof(double) * 2 * ng), *psi = (double *)malloc(sizeof(double) * ng);
+    const double dt = c->dt, qm = q / m;
+    /* terminal: a_x = grad W(x_N), W = 1/2 eps0 dA sum |E|^2 */
+    {
+        const double *xN = X + (size_t)nsteps * n, *yN = Y + (size_t)nsteps * n;
+        adj_fields(&A, xN, yN, ex, ey);
+        for (size_t i = 0; i < ng; ++i) {
+            g[i] = c->eps0 * A.dA * ex[i];
+            g[ng + i] = c->eps0 * A.dA * ey[i];
+        }
+        adj_solve_T(&A, g, g + ng, psi);
+        adj_gather_psi(&A, xN, yN, psi, ax, ay);
+    }
+    for (long st = nsteps - 1; st >= 0; --st) {
+        const double *xs = X + (size_t)st * n, *ys = Y + (size_t)st * n;
+        for (long i = 0; i < n; ++i) {  /* drift adjoint */
+            avx[i] += dt * ax[i];
+            avy[i] += dt * ay[i];
+        }
+        adj_fields(&A, xs, ys, ex, ey);
+        adj_kick(&A, xs, ys, ex, ey, avx, avy, dt * qm, ax, ay);
+    }
+    /* priming v(-1/2) = v0 - (q/m) F(x0) dt/2 */
+    adj_fields(&A, X, Y, ex, ey);
+    adj_kick(&A, X, Y, ex, ey, avx, avy, -0.5 * dt * qm, ax, ay);
+    for (long i = 0; i < n; ++i) {
+        if (gx0) gx0[i] = ax[i];
+        if (gy0) gy0[i] = ay[i];
+        if (gvx0) gvx0[i] = avx[i];
+        if (gvy0) gvy0[i] = avy[i];
+    }
+    free(X);
+    free(Y);
+    free(ax);
+    free(ay);
+    free(avx);
+    free(avy);
+    free(ex);
+    free(ey);
+    free(g);
+    free(psi);
+    return J;
+}

@@ -130,6 +130,23 @@ void orc_dsmc_run(const orc_dsmc *d, long n, double *x, double *y, double *vx, d
                   double *vz, double *sgmax, long nsteps, uint64_t first_pass, double *T_even,
                   double *T_odd, long counts[2]);
 
+/* ---------------- adjoint of the physics step (FP64) ----------------
+ * One species on the physics-mode step: v(-1/2) = v0 - (q/m) E(x0) dt/2,
+ * then nsteps leapfrog steps; J = 1/2 eps0 dA sum |E(x_N)|^2.  Stores the
+ * whole trajectory (test sizes only) and runs the discrete adjoint
+ * backwards: a_v += dt a_x; a_x += [dt (q/m) dF/dx]^T a_v, the transpose made
+ * of the local CIC-gradient term, the scatter of mu = dt (q/m) a_v to the
+ * grid, psi = S^T g (psi^ = i k.g^ / (eps0 k^2)) and the CIC-gradient gather
+ * of psi.  Returns J; writes dJ/dx0, dJ/dy0, dJ/dvx0, dJ/dvy0 (n each, may be
+ * NULL).  x0.. are not modified. */
+double orc_adjoint(const orc_phys_cfg *c, long n, double q, double m, const double *x0,
+                   const double *y0, const double *vx0, const double *vy0, long nsteps,
+                   double *gx0, double *gy0, double *gvx0, double *gvy0, int nthreads);
+/* Forward only, same map: J for the given initial state. */
+double orc_forward_J(const orc_phys_cfg *c, long n, double q, double m, const double *x0,
+                     const double *y0, const double *vx0, const double *vy0, long nsteps,
+                     int nthreads);
+
 #ifdef __cplusplus
 }
 #endif
