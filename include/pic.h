@@ -377,6 +377,35 @@ enum pic_history {
 /* Copy history entries [first, first+count) (steps) to host. */
 pic_status pic_get_history(pic_handle *h, int which, long long first, long long count,
                            double *out);
+
+/* ---- ensembles of independent runs ----
+ * Many independent collisionless runs, each with its own grid, particle
+ * count and load, advanced together: every stage of a step is one launch
+ * over all runs (push, sort, density conversion, k-space kernel, diagnostics
+ * fold), the FFTs are batched over the runs of each grid size, and steps are
+ * replayed from CUDA graphs.  A per-run offset table (particle slots, grid
+ * nodes, spectrum, sort keys) and per-block work tables drive the kernels.
+ * Run r follows runs[r]: nx, ny, Lx, Ly, dt, eps0 and species[0] (one
+ * charged species: capacity, q, m, q_int); its sort tiles are chosen from
+ * its particles per cell.  chunk, halo, sort_every, history and device are
+ * taken from runs[0] (0: the handle defaults).  A run gives the same
+ * particles as a handle created from runs[r] and stepped alike.  No
+ * counterpart in the reference (it runs one simulation per process). */
+typedef struct pic_ensemble pic_ensemble;
+pic_status pic_ensemble_create(const pic_config *runs, int nruns, pic_ensemble **out);
+pic_status pic_ensemble_destroy(pic_ensemble *e);
+pic_status pic_ensemble_get_stream(pic_ensemble *e, void **stream);
+pic_status pic_ensemble_synchronize(pic_ensemble *e);
+/* Load run r from specs[r] (specs[r].n <= its capacity), sort, deposit,
+ * solve, and prime the leapfrog (v to t = -dt/2) of every run. */
+pic_status pic_ensemble_init(pic_ensemble *e, const pic_init_spec *specs);
+pic_status pic_ensemble_step(pic_ensemble *e, long long nsteps);
+pic_status pic_ensemble_diagnostics(pic_ensemble *e, int run, pic_diag *d);
+pic_status pic_ensemble_get_history(pic_ensemble *e, int run, int which, long long first,
+                                    long long count, double *out);
+pic_status pic_ensemble_get_particles(pic_ensemble *e, int run, long long *n, double *x, double *y,
+                                      double *vx, double *vy);
+
 /* Track |rho^| of one Fourier mode each step (PIC_HIST_MODE_AMP). */
 pic_status pic_track_mode(pic_handle *h, int mx, int my);
 

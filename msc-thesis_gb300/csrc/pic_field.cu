@@ -10,31 +10,9 @@
 // zero mode removed (immobile neutralising background) and one 1/N.
 #include <cuda_runtime.h>
 
-#include "pic_internal.cuh"
+#include "pic_field_dev.cuh"
 
 namespace pic {
-
-__device__ __forceinline__ double warp_sum_d(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ __forceinline__ float fixed_to_float(unsigned long long v, long long mean_fix, float scale)
-{
-    // int64 -> float as hi * 2^32 + lo: two 32-bit conversions and one fma
-    // (at most one extra rounding)
-    const long long d = (long long)v - mean_fix;
-    return fmaf((float)(int)(d >> 32), 4294967296.0f, (float)(unsigned)(d & 0xFFFFFFFFll)) * scale;
-}
 
 // rho = (rho_fix - mean) * scale, sum(rho_fix) -> dev->q; rho_fix is cleared
 // by a memset after this kernel.  The background is removed in exact integer
@@ -85,34 +63,23 @@ __global__ void __launch_bounds__(256) kspace_kernel(KspaceArgs A)
 {
     __shared__ double s_part[8];
     const long long total = (long long)A.ny * A.nh;
-    const bool nx_even = (A.nx & 1) == 0, ny_even = (A.ny & 1) == 0;
     float fe = 0.f;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += stride) {
         const int my = (int)(idx / A.nh);
         const int mx = (int)(idx - (long long)my * A.nh);
-        const int sy = (2 * my <= A.ny) ? my : my - A.ny;
-        const float kx = A.kx1 * (float)mx, ky = A.ky1 * (float)sy;
-        const float k2 = kx * kx + ky * ky;
         const float2 r = A.rhohat[idx];
-        const float inv = (idx == 0) ? 0.f : A.inv_eps0_n / k2;
-        const float2 ph = make_float2(r.x * inv, r.y * inv);
+        const KMode K = kspace_mode(r, mx, my, A.nx, A.ny, A.kx1, A.ky1, A.inv_eps0_n, idx == 0);
         if (mx == A.tmx && my == A.tmy)
             A.dev->mode_amp = sqrt((double)r.x * r.x + (double)r.y * r.y) / ((double)A.nx * A.ny);
         if (A.phi_mode) {
-            A.ehat[idx] = ph;
+            A.ehat[idx] = K.ph;
             continue;
         }
-        // E^ = -i k phi^; the Nyquist component of a derivative is set to zero
-        const float kxe = (nx_even && 2 * mx == A.nx) ? 0.f : kx;
-        const float kye = (ny_even && 2 * my == A.ny) ? 0.f : ky;
-        const float2 ex = make_float2(kxe * ph.y, -kxe * ph.x);
-        const float2 ey = make_float2(kye * ph.y, -kye * ph.x);
-        A.ehat[idx] = ex;
-        A.ehat[total + idx] = ey;
-        const float w = (mx == 0 || (nx_even && 2 * mx == A.nx)) ? 1.f : 2.f;
-        fe += w * (ex.x * ex.x + ex.y * ex.y + ey.x * ey.x + ey.y * ey.y);
+        A.ehat[idx] = K.ex;
+        A.ehat[total + idx] = K.ey;
+        fe += K.fe;
     }
     if (A.phi_mode) return;
     double d = warp_sum_d((double)fe);
@@ -125,36 +92,10 @@ __global__ void __launch_bounds__(256) kspace_kernel(KspaceArgs A)
     }
 }
 
-// Moves the accumulators of the finished stage into the history ring and
-// clears them; one warp, lane l folds slot l.  ADV_PUSH closes the particle
-// pass of step s (kinetic energy and momentum belong to step s) and advances
-// the step counter; ADV_FIELD records the field of the current step.
+// diagnostics fold of one handle (one warp)
 __global__ void advance_kernel(DevState *d, double *hist, int cap, int kind, double fe_scale)
 {
-    const int l = threadIdx.x;  // 32 threads = ACC_SLOTS
-    const long long s = d->step;
-    const int k = (int)(s % cap);
-    if (kind == ADV_PUSH) {
-        const double ke = warp_sum_d(d->ke[l]), px = warp_sum_d(d->px[l]), py = warp_sum_d(d->py[l]);
-        d->ke[l] = d->px[l] = d->py[l] = 0.0;
-        if (l == 0) {
-            hist[1 * (size_t)cap + k] = ke;
-            hist[2 * (size_t)cap + k] = px;
-            hist[3 * (size_t)cap + k] = py;
-            d->step = s + 1;
-        }
-    } else {
-        const double fe = warp_sum_d(d->fe[l]);
-        const unsigned long long q = warp_sum_u64(d->q[l]);
-        d->fe[l] = 0.0;
-        d->q[l] = 0ull;
-        if (l == 0) {
-            hist[0 * (size_t)cap + k] = fe * fe_scale;
-            hist[4 * (size_t)cap + k] = (double)(long long)q;
-            hist[5 * (size_t)cap + k] = d->mode_amp;
-            d->mode_amp = 0.0;
-        }
-    }
+    advance_state(d, hist, cap, kind, fe_scale);
 }
 
 pic_status launch_convert(pic_handle *h)

@@ -58,7 +58,7 @@ int grid_for(long long n, int block)
     return (int)b;
 }
 
-static int pick_divisor(int n, int target)
+int pick_divisor(int n, int target)
 {
     if (target < 1) target = 1;
     if (target > n) target = n;
@@ -419,9 +419,9 @@ pic_status handle_reload(pic_handle *h, const long long *n, long long step,
     return refresh(h);
 }
 
-pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly)
+pic_status lattice_dims_for(int nx, int ny, long long n, int *lx, int *ly)
 {
-    const long long nc = (long long)h->g.nx * h->g.ny;
+    const long long nc = (long long)nx * ny;
     if (n % nc) {
         set_error("lattice load needs a whole number of particles per cell");
         return PIC_ERR_INVALID_ARG;
@@ -429,9 +429,14 @@ pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly)
     const long long ppc = n / nc;
     long long a = (long long)std::ceil(std::sqrt((double)ppc));
     while (ppc % a) ++a;  // smallest divisor >= sqrt(ppc): more sites along x
-    *lx = (int)(h->g.nx * a);
-    *ly = (int)(h->g.ny * (ppc / a));
+    *lx = (int)(nx * a);
+    *ly = (int)(ny * (ppc / a));
     return PIC_OK;
+}
+
+pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly)
+{
+    return lattice_dims_for(h->g.nx, h->g.ny, n, lx, ly);
 }
 
 }  // namespace pic

@@ -153,33 +153,59 @@ __global__ void fill_padding_kernel(int32_t *c0, int32_t *c1, long long from, lo
     }
 }
 
-static InitArgs base_args(pic_handle *h, int s)
+static InitArgs target_args(const InitTarget &T)
 {
-    SpeciesBuf &B = h->sp[s];
-    const Geometry &g = h->g;
     InitArgs A;
     memset(&A, 0, sizeof(A));
-    A.cell = B.cell[0];
-    A.ox = B.ox[0];
-    A.oy = B.oy[0];
-    A.vx = B.vx[0];
-    A.vy = B.vy[0];
-    A.vz = B.vz[0];
-    A.pid = B.pid[0];
-    A.nx = g.nx;
-    A.ny = g.ny;
-    A.Lx = g.Lx;
-    A.Ly = g.Ly;
-    A.dx = g.dx;
-    A.dy = g.dy;
-    A.inv_dx = 1.0 / g.dx;
-    A.inv_dy = 1.0 / g.dy;
+    A.cell = T.cell;
+    A.ox = T.ox;
+    A.oy = T.oy;
+    A.vx = T.vx;
+    A.vy = T.vy;
+    A.vz = T.vz;
+    A.pid = T.pid;
+    A.nx = T.nx;
+    A.ny = T.ny;
+    A.Lx = T.Lx;
+    A.Ly = T.Ly;
+    A.dx = T.Lx / T.nx;
+    A.dy = T.Ly / T.ny;
+    A.inv_dx = 1.0 / A.dx;
+    A.inv_dy = 1.0 / A.dy;
     return A;
 }
 
-pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_nx, int lat_ny)
+InitTarget target_of(pic_handle *h, int s)
 {
-    InitArgs A = base_args(h, s);
+    SpeciesBuf &B = h->sp[s];
+    InitTarget T;
+    T.cell = B.cell[0];
+    T.ox = B.ox[0];
+    T.oy = B.oy[0];
+    T.vx = B.vx[0];
+    T.vy = B.vy[0];
+    T.vz = B.vz[0];
+    T.pid = B.pid[0];
+    T.nx = h->g.nx;
+    T.ny = h->g.ny;
+    T.Lx = h->g.Lx;
+    T.Ly = h->g.Ly;
+    return T;
+}
+
+static InitArgs base_args(pic_handle *h, int s)
+{
+    InitArgs A = target_args(target_of(h, s));
+    // the handle's own cell size (identical to L / n up to rounding)
+    A.dx = h->g.dx;
+    A.dy = h->g.dy;
+    A.inv_dx = 1.0 / h->g.dx;
+    A.inv_dy = 1.0 / h->g.dy;
+    return A;
+}
+
+static void spec_args(InitArgs &A, const pic_init_spec *spec, int lat_nx, int lat_ny)
+{
     A.n = spec->n;
     A.layout = spec->layout;
     A.pert_kind = spec->pert_kind;
@@ -192,8 +218,8 @@ pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_
     A.vd1 = spec->vdrift[1];
     A.beam_v = spec->beam_v;
     A.amp = spec->pert_amp;
-    A.kx = 2.0 * 3.14159265358979323846 * spec->pert_mx / h->g.Lx;
-    A.ky = 2.0 * 3.14159265358979323846 * spec->pert_my / h->g.Ly;
+    A.kx = 2.0 * 3.14159265358979323846 * spec->pert_mx / A.Lx;
+    A.ky = 2.0 * 3.14159265358979323846 * spec->pert_my / A.Ly;
     for (int b = 0; b < 2; ++b)
         for (int c = 0; c < 2; ++c) {
             A.xi[b][c] = spec->beam_xi[b][c];
@@ -201,11 +227,30 @@ pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_
         }
     A.k0 = (uint32_t)spec->seed;
     A.k1 = (uint32_t)(spec->seed >> 32);
+}
+
+static pic_status run_init(const InitArgs &A, cudaStream_t st)
+{
     if (A.n > 0) {
-        init_kernel<<<grid_for(A.n, 256), 256, 0, h->stream>>>(A);
+        init_kernel<<<grid_for(A.n, 256), 256, 0, st>>>(A);
         PIC_CUDA(cudaGetLastError());
     }
     return PIC_OK;
+}
+
+pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_nx, int lat_ny)
+{
+    InitArgs A = base_args(h, s);
+    spec_args(A, spec, lat_nx, lat_ny);
+    return run_init(A, h->stream);
+}
+
+pic_status launch_init_target(const InitTarget &T, const pic_init_spec *spec, int lat_nx,
+                              int lat_ny, cudaStream_t st)
+{
+    InitArgs A = target_args(T);
+    spec_args(A, spec, lat_nx, lat_ny);
+    return run_init(A, st);
 }
 
 // d(x, y)/d(pert_amp) of init_kernel's position, in id order.  XDISP:
@@ -238,24 +283,22 @@ __global__ void init_damp_kernel(InitArgs A, double *dxa, double *dya)
     }
 }
 
-pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
-                          double *dxdA, double *dydA)
+pic_status launch_init_dA_target(const InitTarget &T, const pic_init_spec *spec, int lat_nx,
+                                 int lat_ny, double *dxdA, double *dydA, cudaStream_t st)
 {
-    InitArgs A = base_args(h, 0);
-    A.n = spec->n;
-    A.layout = spec->layout;
-    A.pert_kind = spec->pert_kind;
-    A.lat_nx = lat_nx;
-    A.lat_ny = lat_ny;
-    A.kx = 2.0 * 3.14159265358979323846 * spec->pert_mx / h->g.Lx;
-    A.ky = 2.0 * 3.14159265358979323846 * spec->pert_my / h->g.Ly;
-    A.k0 = (uint32_t)spec->seed;
-    A.k1 = (uint32_t)(spec->seed >> 32);
+    InitArgs A = target_args(T);
+    spec_args(A, spec, lat_nx, lat_ny);
     if (A.n > 0) {
-        init_damp_kernel<<<grid_for(A.n, 256), 256, 0, h->stream>>>(A, dxdA, dydA);
+        init_damp_kernel<<<grid_for(A.n, 256), 256, 0, st>>>(A, dxdA, dydA);
         PIC_CUDA(cudaGetLastError());
     }
     return PIC_OK;
+}
+
+pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
+                          double *dxdA, double *dydA)
+{
+    return launch_init_dA_target(target_of(h, 0), spec, lat_nx, lat_ny, dxdA, dydA, h->stream);
 }
 
 pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x_dev,
@@ -280,6 +323,18 @@ pic_status launch_to_global(pic_handle *h, int s, double *x_dev, double *y_dev, 
     to_global_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(
         B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.vz[0], B.pid[0], &h->dev->n[s], h->g.dx,
         h->g.dy, x_dev, y_dev, vx_dev, vy_dev, vz_dev);
+    PIC_CUDA(cudaGetLastError());
+    return PIC_OK;
+}
+
+pic_status launch_to_global_target(const InitTarget &T, const long long *d_n, long long cap,
+                                   double *x_dev, double *y_dev, double *vx_dev, double *vy_dev,
+                                   cudaStream_t st)
+{
+    if (cap == 0) return PIC_OK;
+    to_global_kernel<<<grid_for(cap, 256), 256, 0, st>>>(T.cell, T.ox, T.oy, T.vx, T.vy, nullptr,
+                                                         T.pid, d_n, T.Lx / T.nx, T.Ly / T.ny,
+                                                         x_dev, y_dev, vx_dev, vy_dev, nullptr);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }

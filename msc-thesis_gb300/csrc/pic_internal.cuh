@@ -196,6 +196,11 @@ enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s);
+// exclusive scan of count[0, nkeys) into offset and cursor, offset[nkeys] =
+// *d_total; bsum, bsum_s: ceil(nkeys / 4096) entries, bsum2: ceil(that / 4096)
+pic_status launch_key_scan(const uint32_t *count, uint32_t *offset, uint32_t *cursor,
+                           long long nkeys, uint32_t *bsum, uint32_t *bsum_s, uint32_t *bsum2,
+                           const long long *d_total, cudaStream_t st);
 // pic_collide.cu
 pic_status launch_mcc(pic_handle *h);
 pic_status launch_ntc(pic_handle *h);
@@ -209,6 +214,22 @@ pic_status launch_to_global(pic_handle *h, int s, double *x_dev, double *y_dev, 
 pic_status launch_fill_padding(pic_handle *h, int s, long long from, long long to);
 pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
                           double *dxdA, double *dydA);
+// particle arrays (buffer 0) and grid of one run, for callers without a handle
+struct InitTarget {
+    int32_t *cell;
+    float *ox, *oy, *vx, *vy, *vz;
+    uint32_t *pid;
+    int nx, ny;
+    double Lx, Ly;
+};
+InitTarget target_of(pic_handle *h, int s);
+pic_status launch_init_target(const InitTarget &T, const pic_init_spec *spec, int lat_nx,
+                              int lat_ny, cudaStream_t st);
+pic_status launch_init_dA_target(const InitTarget &T, const pic_init_spec *spec, int lat_nx,
+                                 int lat_ny, double *dxdA, double *dydA, cudaStream_t st);
+pic_status launch_to_global_target(const InitTarget &T, const long long *d_n, long long cap,
+                                   double *x_dev, double *y_dev, double *vx_dev, double *vy_dev,
+                                   cudaStream_t st);
 
 // grid-stride launch size for `n` items on the current device
 int grid_for(long long n, int block);
@@ -220,5 +241,7 @@ pic_status deposit_now(pic_handle *h);
 pic_status refresh(pic_handle *h);
 pic_status ensure_stage(pic_handle *h, size_t bytes);
 pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly);
+pic_status lattice_dims_for(int nx, int ny, long long n, int *lx, int *ly);
+int pick_divisor(int n, int target);
 
 }  // namespace pic

@@ -1,0 +1,322 @@
+// pic_push_dev.cuh -- device functions of the fused gather + push + deposit
+// pass, shared by the single-run kernels (pic_push.cu) and the ensemble
+// kernels (pic_ensemble.cu).  The arithmetic and the work decomposition are
+// described at the top of pic_push.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pic_internal.cuh"
+
+namespace pic {
+
+struct Cic4 {
+    unsigned long long w00, w10, w01, w11;
+};
+
+// Node weights of `cnt` particles in one cell from their sums of fx, fy, fx*fy.
+__device__ __forceinline__ Cic4 cic_weights(unsigned cnt, unsigned sfx, unsigned sfy,
+                                            unsigned long long sxy)
+{
+    Cic4 W;
+    W.w11 = sxy;
+    W.w10 = ((unsigned long long)sfx << 16) - sxy;
+    W.w01 = ((unsigned long long)sfy << 16) - sxy;
+    W.w00 = ((unsigned long long)cnt << 32) - ((unsigned long long)(sfx + sfy) << 16) + sxy;
+    return W;
+}
+
+__device__ __forceinline__ void deposit_global(unsigned long long *rho, int nx, int ny, int cx,
+                                               int cy, const Cic4 &W, unsigned long long q)
+{
+    const int cx1 = (cx + 1 == nx) ? 0 : cx + 1;
+    const int cy1 = (cy + 1 == ny) ? 0 : cy + 1;
+    atomicAdd(rho + (size_t)cy * nx + cx, W.w00 * q);
+    atomicAdd(rho + (size_t)cy * nx + cx1, W.w10 * q);
+    atomicAdd(rho + (size_t)cy1 * nx + cx, W.w01 * q);
+    atomicAdd(rho + (size_t)cy1 * nx + cx1, W.w11 * q);
+}
+
+__device__ __forceinline__ void smem_add(unsigned *lo, unsigned *hi, int i, unsigned long long w)
+{
+    atomicAdd(lo + i, (unsigned)(w & 0xFFFFull));
+    atomicAdd(hi + i, (unsigned)(w >> 16));
+}
+
+// Per-run part of a push pass: the grid, its field and density, the
+// diagnostics, the tile window and the step coefficients.
+struct PushGeo {
+    const float *ex, *ey;
+    unsigned long long *rho;
+    DevState *dev;
+    int nx, ny, tw, th, halo, wcx, wcy;
+    float qm_dt, dtdx, dtdy;
+    unsigned long long qmul;  // q_int as two's complement
+    double ke_scale, p_scale; // m/4, m/2 (0 disables the diagnostics)
+};
+
+// Particle arrays of a push pass (and, for a single run, its PushGeo).
+struct PushArgs {
+    const int32_t *cin;
+    const float *oxin, *oyin, *vxin, *vyin;
+    int32_t *cout;
+    float *oxout, *oyout, *vxout, *vyout;
+    const uint32_t *pidin;  // copied to pidout when non-null (out-of-place pass)
+    uint32_t *pidout;
+    const float *vzin;      // copied to vzout when non-null
+    float *vzout;
+    const int32_t *anchor;
+    const long long *d_n;
+    int chunk;
+    PushGeo geo;
+};
+
+// Shared-memory window of a push block: E (float2) and the split deposit
+// accumulators, anchored at the tile of the block's first particle.
+struct Window {
+    float2 *sE;
+    unsigned *sLo, *sHi;
+    int wx0, wy0, nwx, nw;
+    bool on;
+};
+
+__device__ __forceinline__ Window setup_window(const PushGeo &A, unsigned char *smem, int anc)
+{
+    Window W;
+    W.nwx = A.wcx + 1;
+    W.nw = W.nwx * (A.wcy + 1);
+    W.sE = reinterpret_cast<float2 *>(smem);
+    W.sLo = reinterpret_cast<unsigned *>(smem + (size_t)W.nw * sizeof(float2));
+    W.sHi = W.sLo + W.nw;
+    W.on = anc >= 0;
+    W.wx0 = W.wy0 = 0;
+    if (W.on) {
+        int wx0 = (anc & 0xFFFF) * A.tw - A.halo, wy0 = (anc >> 16) * A.th - A.halo;
+        wx0 %= A.nx;
+        if (wx0 < 0) wx0 += A.nx;
+        wy0 %= A.ny;
+        if (wy0 < 0) wy0 += A.ny;
+        W.wx0 = wx0;
+        W.wy0 = wy0;
+    }
+    return W;
+}
+
+template <bool GATHER, bool DEPOSIT>
+__device__ __forceinline__ void load_window(const PushGeo &A, const Window &W)
+{
+    if (!W.on) return;
+    for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
+        const int a = i % W.nwx, b = i / W.nwx;
+        const int gx = (W.wx0 + a) % A.nx, gy = (W.wy0 + b) % A.ny;
+        if (GATHER) W.sE[i] = make_float2(A.ex[(size_t)gy * A.nx + gx], A.ey[(size_t)gy * A.nx + gx]);
+        if (DEPOSIT) {
+            W.sLo[i] = 0u;
+            W.sHi[i] = 0u;
+        }
+    }
+}
+
+// one group of particles in one cell: window or global
+__device__ __forceinline__ void deposit_group(const PushGeo &A, const Window &W, int cx, int cy,
+                                              const Cic4 &C)
+{
+    int dxl = cx - W.wx0, dyl = cy - W.wy0;
+    if (dxl < 0) dxl += A.nx;
+    if (dyl < 0) dyl += A.ny;
+    if (W.on && dxl < A.wcx && dyl < A.wcy) {
+        const int i = dyl * W.nwx + dxl;
+        smem_add(W.sLo, W.sHi, i, C.w00);
+        smem_add(W.sLo, W.sHi, i + 1, C.w10);
+        smem_add(W.sLo, W.sHi, i + W.nwx, C.w01);
+        smem_add(W.sLo, W.sHi, i + W.nwx + 1, C.w11);
+    } else {
+        deposit_global(A.rho, A.nx, A.ny, cx, cy, C, A.qmul);
+    }
+}
+
+// Gather, push and deposit four consecutive particles held in registers.
+template <bool GATHER, bool DEPOSIT>
+__device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int (&cc)[4],
+                                          float (&xo)[4], float (&yo)[4], float (&xv)[4],
+                                          float (&yv)[4], float &ke, float &px, float &py,
+                                          bool &bad)
+{
+    const int nx = A.nx, ny = A.ny;
+    // register aggregate of the particles that share the first one's new cell
+    unsigned gcnt = 0u, gfx = 0u, gfy = 0u;
+    unsigned long long gxy = 0ull;
+    int gkey = -1, gcx = 0, gcy = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c = cc[j];
+        if (c < 0) continue;  // empty slot
+        int cx = c & 0xFFFF, cy = c >> 16;
+        if (cx >= nx || cy >= ny) {  // corrupt cell: flag, leave untouched
+            bad = true;
+            atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_CELL);
+            continue;
+        }
+        float ox = xo[j], oy = yo[j], vx = xv[j], vy = yv[j];
+        if (GATHER) {
+            const float gx = 1.f - ox, gy = 1.f - oy;
+            float2 e00, e10, e01, e11;
+            int dxl = cx - W.wx0, dyl = cy - W.wy0;
+            if (dxl < 0) dxl += nx;
+            if (dyl < 0) dyl += ny;
+            if (W.on && dxl < A.wcx && dyl < A.wcy) {
+                const int i = dyl * W.nwx + dxl;
+                e00 = W.sE[i];
+                e10 = W.sE[i + 1];
+                e01 = W.sE[i + W.nwx];
+                e11 = W.sE[i + W.nwx + 1];
+            } else {
+                const int cx1 = (cx + 1 == nx) ? 0 : cx + 1;
+                const int cy1 = (cy + 1 == ny) ? 0 : cy + 1;
+                const size_t i00 = (size_t)cy * nx + cx, i10 = (size_t)cy * nx + cx1;
+                const size_t i01 = (size_t)cy1 * nx + cx, i11 = (size_t)cy1 * nx + cx1;
+                e00 = make_float2(A.ex[i00], A.ey[i00]);
+                e10 = make_float2(A.ex[i10], A.ey[i10]);
+                e01 = make_float2(A.ex[i01], A.ey[i01]);
+                e11 = make_float2(A.ex[i11], A.ey[i11]);
+            }
+            const float Ex = gy * fmaf(gx, e00.x, ox * e10.x) + oy * fmaf(gx, e01.x, ox * e11.x);
+            const float Ey = gy * fmaf(gx, e00.y, ox * e10.y) + oy * fmaf(gx, e01.y, ox * e11.y);
+            const float vx0 = vx, vy0 = vy;
+            vx = fmaf(A.qm_dt, Ex, vx);
+            vy = fmaf(A.qm_dt, Ey, vy);
+            ke = fmaf(vx0, vx0, fmaf(vy0, vy0, fmaf(vx, vx, fmaf(vy, vy, ke))));
+            px += vx0 + vx;
+            py += vy0 + vy;
+        } else {
+            ke = fmaf(2.f * vx, vx, fmaf(2.f * vy, vy, ke));
+            px = fmaf(2.f, vx, px);
+            py = fmaf(2.f, vy, py);
+        }
+        bad |= !(fabsf(vx) <= 3.0e38f) || !(fabsf(vy) <= 3.0e38f);
+        // drift in cell units; carry whole cells into the index
+        ox = fmaf(vx, A.dtdx, ox);
+        oy = fmaf(vy, A.dtdy, oy);
+        float sx = floorf(ox), sy = floorf(oy);
+        ox -= sx;
+        oy -= sy;
+        if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
+        if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
+        cx += (int)sx;
+        cy += (int)sy;
+        if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
+        if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
+        const int cn = cx | (cy << 16);
+        cc[j] = cn;
+        xo[j] = ox;
+        yo[j] = oy;
+        xv[j] = vx;
+        yv[j] = vy;
+        if (DEPOSIT) {
+            const unsigned fx = __float2uint_rn(ox * 65536.0f);
+            const unsigned fy = __float2uint_rn(oy * 65536.0f);
+            const unsigned long long fxy = (unsigned long long)fx * fy;
+            if (gkey < 0) {
+                gkey = cn;
+                gcx = cx;
+                gcy = cy;
+            }
+            if (cn == gkey) {
+                ++gcnt;
+                gfx += fx;
+                gfy += fy;
+                gxy += fxy;
+            } else {
+                deposit_group(A, W, cx, cy, cic_weights(1u, fx, fy, fxy));
+            }
+        }
+    }
+    if (DEPOSIT && gcnt) deposit_group(A, W, gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+}
+
+__device__ __forceinline__ void store_quad(const PushArgs &A, long long q, const int (&cc)[4],
+                                           const float (&xo)[4], const float (&yo)[4],
+                                           const float (&xv)[4], const float (&yv)[4])
+{
+    *reinterpret_cast<int4 *>(A.cout + q) = make_int4(cc[0], cc[1], cc[2], cc[3]);
+    *reinterpret_cast<float4 *>(A.oxout + q) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+    *reinterpret_cast<float4 *>(A.oyout + q) = make_float4(yo[0], yo[1], yo[2], yo[3]);
+    *reinterpret_cast<float4 *>(A.vxout + q) = make_float4(xv[0], xv[1], xv[2], xv[3]);
+    *reinterpret_cast<float4 *>(A.vyout + q) = make_float4(yv[0], yv[1], yv[2], yv[3]);
+    if (A.pidin)
+        *reinterpret_cast<uint4 *>(A.pidout + q) = *reinterpret_cast<const uint4 *>(A.pidin + q);
+    if (A.vzin)
+        *reinterpret_cast<float4 *>(A.vzout + q) = *reinterpret_cast<const float4 *>(A.vzin + q);
+}
+
+// end of a block: diagnostics reduction, error flags, window flush
+template <bool DEPOSIT>
+__device__ __forceinline__ void finish_block(const PushGeo &A, const Window &W, double *sAcc,
+                                             float ke, float px, float py, bool bad)
+{
+    if (A.ke_scale != 0.0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ke += __shfl_xor_sync(0xffffffffu, ke, o);
+            px += __shfl_xor_sync(0xffffffffu, px, o);
+            py += __shfl_xor_sync(0xffffffffu, py, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(sAcc + 0, (double)ke);
+            atomicAdd(sAcc + 1, (double)px);
+            atomicAdd(sAcc + 2, (double)py);
+        }
+    }
+    const int any_bad = __syncthreads_or(bad ? 1 : 0);
+    if (threadIdx.x == 0) {
+        if (A.ke_scale != 0.0) {
+            const int sl = acc_slot();
+            atomicAdd(&A.dev->ke[sl], sAcc[0] * A.ke_scale);
+            atomicAdd(&A.dev->px[sl], sAcc[1] * A.p_scale);
+            atomicAdd(&A.dev->py[sl], sAcc[2] * A.p_scale);
+        }
+        if (any_bad) atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_NAN);
+    }
+    if (DEPOSIT && W.on) {
+        for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
+            const unsigned long long v = ((unsigned long long)W.sHi[i] << 16) + W.sLo[i];
+            if (v) {
+                const int a = i % W.nwx, b = i / W.nwx;
+                const int gx = (W.wx0 + a) % A.nx, gy = (W.wy0 + b) % A.ny;
+                atomicAdd(A.rho + (size_t)gy * A.nx + gx, v * A.qmul);
+            }
+        }
+    }
+}
+
+
+// One push block: particles [base, end) of one run (end a multiple of 4 or
+// the end of the padded array), window anchored at tile `anc` (-1: none).
+template <bool GATHER, bool DEPOSIT>
+__device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, unsigned char *smem,
+                                           long long base, long long end, int anc)
+{
+    const Window W = setup_window(G, smem, anc);
+    double *sAcc = reinterpret_cast<double *>(smem + (size_t)W.nw * 16);
+    load_window<GATHER, DEPOSIT>(G, W);
+    if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
+    __syncthreads();
+
+    float ke = 0.f, px = 0.f, py = 0.f;
+    bool bad = false;
+    for (long long q = base + 4ll * threadIdx.x; q < end; q += 4ll * blockDim.x) {
+        // plain (coherent) loads: with an in-place pass the same addresses are stored below
+        const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
+        const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
+        const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
+        const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+        const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+        int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+        float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
+        float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
+        push_quad<GATHER, DEPOSIT>(G, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+        store_quad(A, q, cc, xo, yo, xv, yv);
+    }
+    finish_block<DEPOSIT>(G, W, sAcc, ke, px, py, bad);
+}
+
+}  // namespace pic

@@ -146,6 +146,15 @@ SIGNATURES = {
     "pic_adjoint_run": [_H, _vp, C.c_longlong, C.c_int, _vp, _vp, _vp, _vp,
                         C.POINTER(AdjointResult)],
     "pic_step": [_H, C.c_longlong],
+    "pic_ensemble_create": [C.c_void_p, C.c_int, C.POINTER(_H)],
+    "pic_ensemble_destroy": [_H],
+    "pic_ensemble_get_stream": [_H, C.POINTER(_vp)],
+    "pic_ensemble_synchronize": [_H],
+    "pic_ensemble_init": [_H, C.c_void_p],
+    "pic_ensemble_step": [_H, C.c_longlong],
+    "pic_ensemble_diagnostics": [_H, C.c_int, C.POINTER(Diag)],
+    "pic_ensemble_get_history": [_H, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp],
+    "pic_ensemble_get_particles": [_H, C.c_int, C.POINTER(C.c_longlong), _vp, _vp, _vp, _vp],
     "pic_run_host": [_H, C.c_longlong, _vp, _vp, _vp, _vp, C.c_longlong, C.c_int,
                      _vp, _vp, _vp, _vp],
     "pic_diagnostics": [_H, C.POINTER(Diag)],
@@ -478,6 +487,73 @@ class Handle:
         out = np.empty((self.cfg.ny, self.cfg.nx), np.int64)
         self._c("pic_get_rho_fixed", _ptr(out))
         return out
+
+
+class Ensemble:
+    """Many independent collisionless runs advanced together (pic_ensemble_*):
+    one Config per run (one charged species each); chunk, halo, sort_every,
+    history and device come from the first."""
+
+    def __init__(self, cfgs):
+        self.cfgs = list(cfgs)
+        arr = (Config * len(self.cfgs))(*self.cfgs)
+        h = C.c_void_p()
+        _check(load().pic_ensemble_create(C.addressof(arr), len(self.cfgs), C.byref(h)),
+               "pic_ensemble_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            load().pic_ensemble_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, name, *args):
+        _check(getattr(load(), name)(self.h, *args), name)
+
+    def init(self, specs):
+        arr = (InitSpec * len(specs))(*specs)
+        self._c("pic_ensemble_init", C.addressof(arr))
+
+    def step(self, n=1):
+        self._c("pic_ensemble_step", int(n))
+
+    def synchronize(self):
+        self._c("pic_ensemble_synchronize")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._c("pic_ensemble_get_stream", C.byref(s))
+        return s.value or 0
+
+    def diagnostics(self, run) -> Diag:
+        d = Diag()
+        self._c("pic_ensemble_diagnostics", run, C.byref(d))
+        return d
+
+    def history(self, run, which, first, count):
+        out = np.empty(count)
+        self._c("pic_ensemble_get_history", run, which, first, count, _ptr(out))
+        return out
+
+    def get_particles(self, run):
+        n = C.c_longlong()
+        self._c("pic_ensemble_get_particles", run, C.byref(n), None, None, None, None)
+        a = {k: np.empty(n.value) for k in ("x", "y", "vx", "vy")}
+        self._c("pic_ensemble_get_particles", run, C.byref(n), *[_ptr(a[k]) for k in
+                                                                ("x", "y", "vx", "vy")])
+        return a
 
 
 def field_energy_function(handle: Handle, nsteps: int, every: int = 10):

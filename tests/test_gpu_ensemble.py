@@ -1,0 +1,116 @@
+"""Ensembles (pic_ensemble_*) against the same runs on single handles and
+against the FP64 oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+import picgpu as P
+from gpu_util import normalized_electrons, oracle_from_handle, periodic_diff
+
+pytestmark = pytest.mark.gpu
+
+L = 4 * np.pi
+DT = 0.1
+# (nx, ny, particles per cell, beam drift, x-displacement amplitude, seed)
+RUNS = [(32, 32, 16, 0.2, 1e-3, 1), (64, 32, 8, 0.15, 3e-3, 2), (32, 32, 32, 0.3, 1e-4, 3),
+        (16, 64, 16, 0.1, 1e-2, 4), (64, 64, 4, 0.25, 5e-4, 5)]
+
+
+def run_cfg(nx, ny, ppc, **tuning):
+    n = nx * ny * ppc
+    cfg, q, m = normalized_electrons(nx, ny, L, L, n, DT, **tuning)
+    return cfg, n, q, m
+
+
+def run_spec(n, v0, amp, seed):
+    return P.init_spec(n, vth=(0.01, 0.01, 0.0), beam_v=v0, pert_kind=P.PERT_XDISP, pert_amp=amp,
+                       pert_mx=1, seed=seed)
+
+
+def build(runs, **tuning):
+    cfgs, specs = [], []
+    for nx, ny, ppc, v0, amp, seed in runs:
+        cfg, n, _, _ = run_cfg(nx, ny, ppc, **tuning)
+        cfgs.append(cfg)
+        specs.append(run_spec(n, v0, amp, seed))
+    return cfgs, specs
+
+
+def test_ensemble_runs_match_single_handles():
+    nst = 30
+    cfgs, specs = build(RUNS, sort_every=5, chunk=1024)
+    with P.Ensemble(cfgs) as E:
+        E.init(specs)
+        E.step(nst)
+        E.synchronize()
+        ens = [E.get_particles(r) for r in range(len(RUNS))]
+        fe_ens = [E.history(r, P.HIST_FIELD_ENERGY, 0, nst + 1) for r in range(len(RUNS))]
+        diags = [E.diagnostics(r) for r in range(len(RUNS))]
+    exact = 0
+    for r, (cfg, spec) in enumerate(zip(cfgs, specs)):
+        with P.Handle(cfg) as h:
+            h.init_particles(0, spec)
+            h.prime_leapfrog()
+            h.step(nst)
+            a = h.get_particles(0)
+            fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
+        dx = L / cfg.nx
+        err = max(np.abs(periodic_diff(ens[r]["x"], a["x"], L)).max(),
+                  np.abs(periodic_diff(ens[r]["y"], a["y"], L)).max()) / dx
+        same = all(np.array_equal(ens[r][k], a[k]) for k in a)
+        exact += same
+        print(f"run {r}: {cfg.nx}x{cfg.ny}, max position difference {err:.2e} cells, "
+              f"bit-identical {same}, FE rel diff {np.max(np.abs(fe_ens[r] - fe) / fe.max()):.2e}")
+        assert err < 1e-4
+        np.testing.assert_allclose(ens[r]["vx"], a["vx"], atol=1e-5)
+        np.testing.assert_allclose(fe_ens[r], fe, rtol=1e-5, atol=1e-6 * fe.max())
+        d = diags[r]
+        assert d.step == nst and d.error_flags == 0
+        assert d.total_charge_fixed == d.expected_charge_fixed
+    print("bit-identical runs:", exact, "of", len(RUNS))
+
+
+def test_ensemble_independent_of_sort_cadence():
+    cfgs1, specs = build(RUNS[:3], sort_every=1, chunk=512)
+    cfgs2, _ = build(RUNS[:3], sort_every=7, chunk=2048)
+    out = []
+    for cfgs in (cfgs1, cfgs2):
+        with P.Ensemble(cfgs) as E:
+            E.init(specs)
+            E.step(20)
+            out.append([E.get_particles(r) for r in range(3)])
+    for r in range(3):
+        for k in out[0][r]:
+            np.testing.assert_array_equal(out[0][r][k], out[1][r][k], err_msg=f"run {r} {k}")
+
+
+def test_ensemble_field_energy_matches_fp64_oracle():
+    runs = [(32, 32, 16, 0.2, 1e-2, 7), (16, 32, 32, 0.25, 1e-2, 8)]
+    nst = 40
+    cfgs, specs = build(runs)
+    with P.Ensemble(cfgs) as E:
+        E.init(specs)
+        E.step(nst)
+        fe_ens = [E.history(r, P.HIST_FIELD_ENERGY, 0, nst + 1) for r in range(len(runs))]
+    for r, (nx, ny, ppc, v0, amp, seed) in enumerate(runs):
+        cfg, n, q, m = run_cfg(nx, ny, ppc)
+        with P.Handle(cfg) as h:
+            h.init_particles(0, specs[r])
+            st = oracle_from_handle(h, cfg, q, m)
+        st.prime(nthreads=0)
+        ref = st.run(nst, nthreads=0)
+        rel = np.abs(fe_ens[r] - ref["fe"]) / ref["fe"].max()
+        print(f"run {r}: field energy max rel error vs FP64 oracle {rel.max():.2e}")
+        assert rel.max() < 1e-4
+
+
+def test_ensemble_rejects_bad_configs():
+    cfg, n, _, _ = run_cfg(32, 32, 4)
+    two = P.config(32, 32, L, L, DT, [P.species(n, -1.0, 1.0, -1), P.species(n, 1.0, 1.0, 1)])
+    with pytest.raises(P.PicError):
+        P.Ensemble([cfg, two])
+    with P.Ensemble([cfg]) as E:
+        with pytest.raises(P.PicError):
+            E.step(1)  # not initialised
+        with pytest.raises(P.PicError):
+            E.init([run_spec(n + 4, 0.2, 1e-3, 1)])  # over capacity
