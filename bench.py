@@ -120,21 +120,29 @@ def dist_env():
     return rank, world, local
 
 
-def launches_for(k, since_sort, S, nspecies=1):
-    """Our kernels launched by pic_step(k), following its schedule: per step
-    nspecies pushes + 2 advance + convert + kspace; per sort and species
-    histogram, 3 scan kernels and the scatter.  Returns (count, since_sort)."""
-    n, cnt = k, 0
+def schedule(k, since_sort, S):
+    """Sorts and steps of pic_step(k) / pic_ensemble_step(k) from a given
+    count of steps since the last sort: a sort (+ S steps) whenever S steps
+    have passed.  Returns (sorts, since_sort after)."""
+    n, sorts = k, 0
     while n > 0:
         if since_sort >= S:
-            sorts, steps = 1, (S if n >= S else 1)
+            sorts += 1
+            steps = S if n >= S else 1
             since_sort = steps
         else:
-            sorts, steps = 0, 1
+            steps = 1
             since_sort += 1
-        cnt += sorts * 5 * nspecies + steps * (nspecies + 4)
         n -= steps
-    return cnt, since_sort
+    return sorts, since_sort
+
+
+def launches_for(k, since_sort, S, nspecies=1, per_sort=6):
+    """Our kernels launched by k steps: per step nspecies pushes + 2 advance +
+    convert + kspace; per sort and species histogram, 3 scan kernels, the
+    scatter and the anchor kernel.  Returns (count, sorts, since_sort)."""
+    sorts, after = schedule(k, since_sort, S)
+    return sorts * per_sort * nspecies + k * (nspecies + 4), sorts, after
 
 
 def cpu_sample(nthreads):
@@ -191,11 +199,126 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def c5_runs(P, seed=0, nruns=64, local=0):
+    """The batched two-stream ensemble: grids from {64,128,256,512}^2,
+    particles per cell from {16,...,256}, beam drift U[0.1, 0.3], x-displacement
+    amplitude log-U[1e-4, 1e-2] in mode 1 (k = 0.5, L = 4 pi), vth 0.01,
+    dt 0.1; seeded choices per run."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    grids = rng.choice([64, 128, 256, 512], nruns)
+    ppcs = rng.choice([16, 32, 64, 128, 256], nruns)
+    drift = rng.uniform(0.1, 0.3, nruns)
+    amp = np.exp(rng.uniform(np.log(1e-4), np.log(1e-2), nruns))
+    Lc = 4 * np.pi
+    cfgs, specs = [], []
+    for r in range(nruns):
+        g, ppc = int(grids[r]), int(ppcs[r])
+        n = g * g * ppc
+        A = Lc * Lc
+        cfgs.append(P.config(g, g, Lc, Lc, 0.1, [P.species(n, -A / n, A / n, -1)], device=local))
+        specs.append(P.init_spec(n, vth=(0.01, 0.01, 0.0), beam_v=float(drift[r]),
+                                 pert_kind=P.PERT_XDISP, pert_amp=float(amp[r]), pert_mx=1,
+                                 seed=1000 + r))
+    return cfgs, specs, grids, ppcs
+
+
+def bench_ensemble(args):
+    """Ensemble of 64 runs: one batched ensemble against the same runs one at
+    a time on single handles (each with its own autotuned chunk and cadence)."""
+    import numpy as np
+    import torch
+
+    import picgpu as P
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    cfgs, specs, grids, ppcs = c5_runs(P, local=local)
+    total = sum(int(s.n) for s in specs)
+    tune = None
+    if args.no_tune:
+        cfgs[0].chunk, cfgs[0].sort_every = args.chunk or 8192, args.sort_every
+    else:
+        tune = P.ensemble_autotune(cfgs, specs, trial_steps=10)
+    hbm, peak_kind = peaks()
+    with P.Ensemble(cfgs) as E:
+        E.init(specs)
+        stream = torch.cuda.ExternalStream(E.stream())
+        E.step(args.warmup)
+        E.synchronize()
+        clocks = Clocks(local)
+        clocks.start()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        E.step(args.steps)
+        e1.record(stream)
+        E.synchronize()
+        ms = e0.elapsed_time(e1)
+        clk = clocks.stop()
+        charge_ok = all(E.diagnostics(r).total_charge_fixed == E.diagnostics(r).expected_charge_fixed
+                        for r in range(len(cfgs)))
+    ens_value = total * args.steps / (ms / 1000.0)
+    S = int(cfgs[0].sort_every)
+    _, _, since_w = launches_for(args.warmup, 0, S)
+    nb1 = -(-sum(int(g) * int(g) + 1 for g in grids) // 4096)
+    per_sort = 6 if nb1 <= 4096 else 8  # two-level scan above 4096 block sums
+    ens_launches, ens_sorts, _ = launches_for(args.steps, since_w, S, per_sort=per_sort)
+    # the same runs one at a time (plain handles, autotuned per grid and density)
+    tuned = {}
+    plain_ms = 0.0
+    for cfg, spec, g, ppc in zip(cfgs, specs, grids, ppcs) if not args.no_plain else []:
+        cfg.chunk, cfg.sort_every = 0, 0
+        key = (int(g), int(ppc))
+        if key not in tuned:
+            r = P.autotune(cfg, 0, spec, trial_steps=10)
+            tuned[key] = (r.chunk, r.tile_w, r.tile_h, r.sort_every)
+        cfg.chunk, cfg.tile_w, cfg.tile_h, cfg.sort_every = tuned[key]
+        with P.Handle(cfg) as h:
+            h.init_particles(0, spec)
+            h.prime_leapfrog()
+            st = torch.cuda.ExternalStream(h.stream())
+            h.step(args.warmup)
+            h.synchronize()
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(st)
+            h.step(args.steps)
+            a1.record(st)
+            h.synchronize()
+            plain_ms += a0.elapsed_time(a1)
+    plain_value = total * args.steps / (plain_ms / 1000.0) if plain_ms else None
+    cells = int(sum(int(g) * int(g) for g in grids))
+    step_bytes = BYTES_PER_PARTICLE * total + BYTES_PER_CELL * cells
+    achieved = step_bytes * args.steps / (ms / 1000.0) / 1e9
+    print(json.dumps({
+        "metric": METRIC, "value": ens_value, "unit": "particle-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "ensemble-64-two-stream", "runs": len(cfgs), "particles": total,
+                   "cells": cells, "grid_counts": {str(k): int((grids == k).sum()) for k in (64, 128, 256, 512)},
+                   "chunk": int(cfgs[0].chunk), "sort_every": S, "sorts_in_timed_steps": ens_sorts,
+                   "tune_ms_per_step": tune.ms_per_step if tune else None,
+                   "charge_exact": charge_ok,
+                   "l2": "inputs larger than L2", "peak_kind": peak_kind},
+        "plain_sequential": {"value": plain_value, "unit": "particle-steps/s",
+                             "ms_per_step": plain_ms / args.steps,
+                             "tuned": {f"{k[0]}^2x{k[1]}": v for k, v in tuned.items()}},
+        "speedup_vs_plain": ens_value / plain_value if plain_value else None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "kernel": "whole ensemble step"},
+        "cpu_baseline": None, "e2e": None,
+        "gpu_launches": ens_launches, "clocks": clk}), flush=True)
+
+
 def main():
     global NX, NY, N, L, SORT_EVERY
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=80)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
@@ -206,6 +329,10 @@ def main():
     ap.add_argument("--sort-every", type=int, default=SORT_EVERY)
     ap.add_argument("--push-variant", type=int, default=0, help="0 auto, 1 direct, 2 bulk copy")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (untimed setup)")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="ensemble workload: skip the one-run-at-a-time comparison")
+    ap.add_argument("--workload", default="landau", choices=["landau", "ensemble"],
+                    help="landau: the 2048^2 run (default); ensemble: 64 batched two-stream runs")
     args = ap.parse_args()
     NX = NY = args.nx
     N = NX * NY * PPC
@@ -215,6 +342,9 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "ensemble":
+        bench_ensemble(args)
         return
 
     import numpy as np
@@ -326,8 +456,8 @@ def main():
         cpu = {"value": v, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
                "sample": desc + ", 2 steps"}
 
-    _, since_after_warmup = launches_for(args.warmup, 0, SORT_EVERY)
-    launches, _ = launches_for(args.steps, since_after_warmup, SORT_EVERY)
+    _, _, since_after_warmup = launches_for(args.warmup, 0, SORT_EVERY)
+    launches, sorts_timed, _ = launches_for(args.steps, since_after_warmup, SORT_EVERY)
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -336,6 +466,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": f"landau-{NX}x{NY}-{PPC}ppc", "nx": NX, "ny": NY,
                        "particles": N, "dt": DT, "sort_every": SORT_EVERY,
+                       "sorts_in_timed_steps": sorts_timed,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (2.7 GB particle arrays per step)",
                        "hbm_frac_step": step_bytes * args.steps / (ms_max / 1000.0) / 1e9 / hbm,

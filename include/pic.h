@@ -123,7 +123,9 @@ typedef struct pic_config {
     int halo;            /* shared-memory window halo in cells (0: 2)         */
     int history;         /* diagnostic history length in steps (0: 4096)      */
     int device;          /* CUDA device ordinal                               */
-    int push_variant;    /* 0: auto, 1: direct 128-bit loads, 2: bulk-copy pipeline */
+    int push_variant;    /* 0: auto (1), 1: direct 128-bit loads, 2: bulk-copy
+                            pipeline, 3: direct loads with deposit groups
+                            summed across the warp                           */
 } pic_config;
 
 typedef struct pic_handle pic_handle;
@@ -339,7 +341,7 @@ typedef struct pic_tune_result {
  * *cfg, species `species` is loaded from *spec, the leapfrog primed and
  * `trial_steps` steps (rounded up to whole sort periods) timed with CUDA
  * events after one warm-up period.  Chunk is searched first (4096, 8192,
- * 16384) at the configured cadence, then the cadence (10, 20, 40, 80).  The
+ * 16384) at the configured cadence, then the cadence (2, 5, 10, 20, 40, 80).  The
  * chosen values are written into *cfg.  Needs the memory of one handle at a
  * time. */
 pic_status pic_autotune(pic_config *cfg, int species, const pic_init_spec *spec,
@@ -405,6 +407,14 @@ pic_status pic_ensemble_get_history(pic_ensemble *e, int run, int which, long lo
                                     long long count, double *out);
 pic_status pic_ensemble_get_particles(pic_ensemble *e, int run, long long *n, double *x, double *y,
                                       double *vx, double *vy);
+/* Pick the push chunk (and with it every run's sort tile) and the sort
+ * cadence of an ensemble by timing short runs of it, as pic_autotune does
+ * for one handle: chunk from (2048, 4096, 8192, 16384), then cadence from
+ * (1, 2, 3, 5, 10, 20).  The chosen chunk and sort_every are written into
+ * runs[0]; out->tile_w/tile_h are 0 (tiles differ per run).  Needs the
+ * memory of one ensemble at a time. */
+pic_status pic_ensemble_autotune(pic_config *runs, int nruns, const pic_init_spec *specs,
+                                 int trial_steps, pic_tune_result *out);
 
 /* Track |rho^| of one Fourier mode each step (PIC_HIST_MODE_AMP). */
 pic_status pic_track_mode(pic_handle *h, int mx, int my);

@@ -35,7 +35,7 @@
 namespace pic {
 
 struct EnsRun {
-    int nx, ny, nh, tw, th, ntx, nty, wcx, wcy, halo;
+    int nx, ny, nh, tw, th, ntx, nty, wcx, wcy, hx, hy;
     int key_off;
     long long n, cap4, poff, goff, ncp, khoff, nk;
     float qm_dt, dtdx, dtdy, rho_scale;
@@ -72,7 +72,8 @@ ens_push_kernel(PushArgs A, const SegBlock *__restrict__ blk, const EnsRun *__re
     G.ny = R.ny;
     G.tw = R.tw;
     G.th = R.th;
-    G.halo = R.halo;
+    G.hx = R.hx;
+    G.hy = R.hy;
     G.wcx = R.wcx;
     G.wcy = R.wcy;
     G.qm_dt = R.qm_dt * kick;
@@ -81,7 +82,7 @@ ens_push_kernel(PushArgs A, const SegBlock *__restrict__ blk, const EnsRun *__re
     G.qmul = R.qmul;
     G.ke_scale = drift > 0.f ? R.ke_scale : 0.0;
     G.p_scale = R.p_scale;
-    push_block<GATHER, DEPOSIT>(A, G, smem, b.base, b.base + b.count, anchor[blockIdx.x]);
+    push_block<GATHER, DEPOSIT, false>(A, G, smem, b.base, b.base + b.count, anchor[blockIdx.x]);
 }
 
 __device__ __forceinline__ KeyGeo run_geo(const EnsRun &R)
@@ -97,11 +98,12 @@ ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun 
     sort_hist_block(A, run_geo(runs[b.run]), S, b.base, b.base + b.count);
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 5)
+__global__ void __launch_bounds__(SORT_THREADS, 4)
 ens_sort_scatter_kernel(SortArgs A, const SegBlock *__restrict__ blk,
                         const EnsRun *__restrict__ runs)
 {
-    __shared__ SortSmem S;
+    extern __shared__ __align__(16) unsigned char smem[];
+    ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem);
     const SegBlock b = blk[blockIdx.x];
     sort_scatter_block(A, run_geo(runs[b.run]), S, b.base, b.base + b.count);
 }
@@ -238,7 +240,7 @@ struct pic_ensemble {
     };
     std::vector<Group> groups;
     // graphs
-    cudaGraphExec_t g_one = nullptr, g_period = nullptr;
+    cudaGraphExec_t g_one = nullptr, g_period = nullptr, g_sortstep = nullptr;
     int since_sort = 0;
     bool ready = false;
     // export staging
@@ -252,6 +254,11 @@ pic_status ens_bad(const std::string &m)
 {
     set_error("pic_ensemble_create: " + m);
     return PIC_ERR_INVALID_ARG;
+}
+
+size_t window_smem(const EnsRun &R)
+{
+    return (size_t)(R.wcx + 1) * (R.wcy + 1) * 16 + 32;
 }
 
 void ens_free(pic_ensemble *E)
@@ -272,6 +279,7 @@ void ens_free(pic_ensemble *E)
     }
     if (E->g_one) cudaGraphExecDestroy(E->g_one);
     if (E->g_period) cudaGraphExecDestroy(E->g_period);
+    if (E->g_sortstep) cudaGraphExecDestroy(E->g_sortstep);
     if (E->stream) cudaStreamDestroy(E->stream);
     delete E;
 }
@@ -330,12 +338,10 @@ pic_status ens_layout(pic_ensemble *E)
         R.th = pick_divisor(c.ny, std::max(1, tcells / R.tw));
         R.ntx = c.nx / R.tw;
         R.nty = c.ny / R.th;
-        R.halo = E->halo;
-        R.wcx = 2 * R.tw + 2 * R.halo;
-        R.wcy = R.th + 2 * R.halo;
-        const size_t sm = (size_t)(R.wcx + 1) * (R.wcy + 1) * 16 + 32;
-        if (sm > 48 * 1024) return ens_bad("shared-memory window too large for a run");
-        E->push_smem = std::max(E->push_smem, sm);
+        R.hx = R.hy = E->halo;
+        R.wcx = 2 * R.tw + 2 * R.hx;
+        R.wcy = R.th + 2 * R.hy;
+        if (window_smem(R) > 48 * 1024) return ens_bad("shared-memory window too large for a run");
         R.cap4 = (D.capacity + 3) & ~3ll;
         R.poff = poff;
         R.ncp = (ncell + 3) & ~3ll;
@@ -387,6 +393,37 @@ pic_status ens_layout(pic_ensemble *E)
         s = t;
     }
     return PIC_OK;
+}
+
+// Window halos from the fastest particles of each run's load: the halo
+// along an axis covers half the drift of a sort period (the mean
+// displacement at which a particle is pushed), at least the configured halo,
+// as far as the 48 KB shared-memory window allows.
+void ens_windows(pic_ensemble *E, const pic_init_spec *specs)
+{
+    E->push_smem = 0;
+    for (int s = 0; s < E->nruns; ++s) {
+        EnsRun &R = E->runs[s];
+        const int r = E->run_of[s];
+        const pic_init_spec &S = specs[r];
+        const double dt = E->cfg[r].dt;
+        double ux = std::fabs(S.vdrift[0]) + std::fabs(S.beam_v) + 4.0 * std::fabs(S.vth[0]);
+        for (int b = 0; b < 2; ++b) ux += std::hypot(S.beam_u[b][0], S.beam_u[b][1]);
+        const double uy = std::fabs(S.vdrift[1]) + 4.0 * std::fabs(S.vth[1]);
+        const double half = 0.5 * E->sort_every * dt;
+        R.hx = std::max(E->halo, std::min(24, (int)std::ceil(ux * half / R.dx)));
+        R.hy = std::max(E->halo, std::min(24, (int)std::ceil(uy * half / R.dy)));
+        for (;;) {
+            R.wcx = 2 * R.tw + 2 * R.hx;
+            R.wcy = R.th + 2 * R.hy;
+            if (window_smem(R) <= 48 * 1024 || (R.hx <= E->halo && R.hy <= E->halo)) break;
+            if (R.hx >= R.hy && R.hx > E->halo)
+                --R.hx;
+            else
+                --R.hy;
+        }
+        E->push_smem = std::max(E->push_smem, window_smem(R));
+    }
 }
 
 // push blocks need the particle counts, known at init
@@ -533,7 +570,8 @@ pic_status ens_sort(pic_ensemble *E)
     PIC_CUDA(cudaGetLastError());
     PIC_TRY(launch_key_scan(E->count, E->offset, E->cursor, E->nkeys, E->bsum, E->bsum_s, E->bsum2,
                             E->d_total, st));
-    ens_sort_scatter_kernel<<<E->nsort, SORT_THREADS, 0, st>>>(A, E->sort_blk, E->d_runs);
+    PIC_TRY(scatter_smem_attr((const void *)ens_sort_scatter_kernel));
+    ens_sort_scatter_kernel<<<E->nsort, SORT_THREADS, SCATTER_SMEM, st>>>(A, E->sort_blk, E->d_runs);
     PIC_CUDA(cudaGetLastError());
     if (E->npush) {
         ens_anchor_kernel<<<(E->npush + 255) / 256, 256, 0, st>>>(E->cell[1], E->push_blk, E->d_runs,
@@ -571,8 +609,13 @@ pic_status ens_graphs(pic_ensemble *E)
 {
     if (E->g_one) cudaGraphExecDestroy(E->g_one);
     if (E->g_period) cudaGraphExecDestroy(E->g_period);
-    E->g_one = E->g_period = nullptr;
+    if (E->g_sortstep) cudaGraphExecDestroy(E->g_sortstep);
+    E->g_one = E->g_period = E->g_sortstep = nullptr;
     PIC_TRY(ens_capture(E, &E->g_one, [&] { return ens_step_body(E, 0); }));
+    PIC_TRY(ens_capture(E, &E->g_sortstep, [&] {
+        PIC_TRY(ens_sort(E));
+        return ens_step_body(E, 1);
+    }));
     PIC_TRY(ens_capture(E, &E->g_period, [&] {
         PIC_TRY(ens_sort(E));
         PIC_TRY(ens_step_body(E, 1));
@@ -742,6 +785,7 @@ pic_status pic_ensemble_init(pic_ensemble *e, const pic_init_spec *specs)
     PIC_CUDA(cudaStreamSynchronize(st));
     const size_t ns = (size_t)e->nslots;
     for (int b = 0; b < 2; ++b) PIC_CUDA(cudaMemsetAsync(e->cell[b], 0xFF, ns * 4, st));
+    ens_windows(e, specs);
     PIC_TRY(ens_push_table(e, n_slot));
     std::vector<DevState> z(e->nruns);
     memset(z.data(), 0, sizeof(DevState) * z.size());
@@ -794,10 +838,16 @@ pic_status pic_ensemble_step(pic_ensemble *e, long long nsteps)
     const int S = e->sort_every;
     long long n = nsteps;
     while (n > 0) {
-        if (e->since_sort >= S && n >= S) {
-            PIC_CUDA(cudaGraphLaunch(e->g_period, e->stream));
-            n -= S;
-            e->since_sort = S;
+        if (e->since_sort >= S) {
+            if (n >= S) {
+                PIC_CUDA(cudaGraphLaunch(e->g_period, e->stream));
+                n -= S;
+                e->since_sort = S;
+            } else {
+                PIC_CUDA(cudaGraphLaunch(e->g_sortstep, e->stream));
+                n -= 1;
+                e->since_sort = 1;
+            }
         } else {
             PIC_CUDA(cudaGraphLaunch(e->g_one, e->stream));
             n -= 1;
@@ -903,3 +953,90 @@ pic_status pic_ensemble_get_particles(pic_ensemble *e, int run, long long *n, do
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ autotuner
+namespace {
+
+pic_status ens_time_candidate(const std::vector<pic_config> &runs, const pic_init_spec *specs,
+                              int trial_steps, double *ms)
+{
+    pic_ensemble *e = nullptr;
+    PIC_TRY(pic_ensemble_create(runs.data(), (int)runs.size(), &e));
+    pic_status st = pic_ensemble_init(e, specs);
+    const int S = e->sort_every;
+    const long long steps = ((long long)(trial_steps + S - 1) / S) * S;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (st == PIC_OK) st = pic_ensemble_step(e, 2 * S);  // warm-up (a sort period)
+    if (st == PIC_OK) st = pic_ensemble_synchronize(e);
+    if (st == PIC_OK && cudaEventCreate(&e0) != cudaSuccess) st = PIC_ERR_CUDA;
+    if (st == PIC_OK && cudaEventCreate(&e1) != cudaSuccess) st = PIC_ERR_CUDA;
+    if (st == PIC_OK) {
+        cudaEventRecord(e0, e->stream);
+        st = pic_ensemble_step(e, steps);
+        cudaEventRecord(e1, e->stream);
+        if (st == PIC_OK) st = pic_ensemble_synchronize(e);
+        float t = 0.f;
+        if (st == PIC_OK && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess)
+            *ms = t / (double)steps;
+        else if (st == PIC_OK)
+            st = PIC_ERR_CUDA;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    pic_ensemble_destroy(e);
+    return st;
+}
+
+}  // namespace
+
+extern "C" pic_status pic_ensemble_autotune(pic_config *runs, int nruns, const pic_init_spec *specs,
+                                            int trial_steps, pic_tune_result *out)
+{
+    if (!runs || nruns < 1 || !specs || trial_steps < 1) {
+        set_error("pic_ensemble_autotune: null argument, no runs or trial_steps < 1");
+        return PIC_ERR_INVALID_ARG;
+    }
+    std::vector<pic_config> cur(runs, runs + nruns);
+    if (!cur[0].sort_every) cur[0].sort_every = 20;
+    double best_ms = 1e300;
+    int best_chunk = 0, best_se = cur[0].sort_every, tried = 0;
+    for (int c : {2048, 4096, 8192, 16384}) {
+        cur[0].chunk = c;
+        double ms = 0.0;
+        const pic_status st = ens_time_candidate(cur, specs, trial_steps, &ms);
+        if (st == PIC_ERR_INVALID_ARG) continue;  // a run's window too large for this chunk
+        if (st != PIC_OK) return st;
+        ++tried;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_chunk = c;
+        }
+    }
+    if (!tried) {
+        set_error("pic_ensemble_autotune: no candidate could be created");
+        return PIC_ERR_INVALID_ARG;
+    }
+    cur[0].chunk = best_chunk;
+    const int first_se = cur[0].sort_every;
+    for (int se : {1, 2, 3, 5, 10, 20}) {
+        if (se == first_se) continue;
+        cur[0].sort_every = se;
+        double ms = 0.0;
+        PIC_TRY(ens_time_candidate(cur, specs, trial_steps, &ms));
+        ++tried;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_se = se;
+        }
+    }
+    runs[0].chunk = best_chunk;
+    runs[0].sort_every = best_se;
+    if (out) {
+        out->chunk = best_chunk;
+        out->tile_w = out->tile_h = 0;
+        out->sort_every = best_se;
+        out->ms_per_step = best_ms;
+        out->tried = tried;
+    }
+    return PIC_OK;
+}

@@ -181,7 +181,7 @@ static pic_status setup_geometry(pic_handle *h)
     }
     // the bulk-copy pipeline streams whole stages of 1024 particles
     const bool bulk_ok = (g.chunk % 1024) == 0 && push_bulk_smem(g) <= 200 * 1024;
-    if (c.push_variant < 0 || c.push_variant > 2 || (c.push_variant == 2 && !bulk_ok)) {
+    if (c.push_variant < 0 || c.push_variant > 3 || (c.push_variant == 2 && !bulk_ok)) {
         set_error("pic_create: push_variant 2 needs chunk a multiple of 1024 and a smaller window");
         return PIC_ERR_INVALID_ARG;
     }

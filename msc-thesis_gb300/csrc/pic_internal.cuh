@@ -196,6 +196,7 @@ enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s);
+pic_status scatter_smem_attr(const void *kernel);
 // exclusive scan of count[0, nkeys) into offset and cursor, offset[nkeys] =
 // *d_total; bsum, bsum_s: ceil(nkeys / 4096) entries, bsum2: ceil(that / 4096)
 pic_status launch_key_scan(const uint32_t *count, uint32_t *offset, uint32_t *cursor,

@@ -36,7 +36,7 @@
 namespace pic {
 
 // Direct-load variant: each thread loads its quads with 128-bit loads.
-template <bool GATHER, bool DEPOSIT>
+template <bool GATHER, bool DEPOSIT, bool AGG>
 __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -44,8 +44,8 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
     const long long base = (long long)blockIdx.x * A.chunk;
     if (base >= n) return;  // block-uniform
     const long long n4 = (n + 3) & ~3ll;
-    push_block<GATHER, DEPOSIT>(A, A.geo, smem, base, min(base + (long long)A.chunk, n4),
-                                A.anchor[blockIdx.x]);
+    push_block<GATHER, DEPOSIT, AGG>(A, A.geo, smem, base, min(base + (long long)A.chunk, n4),
+                                     A.anchor[blockIdx.x]);
 }
 
 // ------------------------------------------------------------------------
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256) push_kernel_bulk(PushArgs A)
             int cc[4] = {c4.x, c4.y, c4.z, c4.w};
             float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
             float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
-            push_quad<GATHER, DEPOSIT>(A.geo, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+            push_quad<GATHER, DEPOSIT, false>(A.geo, W, cc, xo, yo, xv, yv, ke, px, py, bad);
             store_quad(A, s0 + l, cc, xo, yo, xv, yv);
         }
         __syncthreads();  // every thread is done with this stage's buffer
@@ -285,7 +285,8 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
     A.geo.ny = g.ny;
     A.geo.tw = g.tw;
     A.geo.th = g.th;
-    A.geo.halo = g.halo;
+    A.geo.hx = g.halo;
+    A.geo.hy = g.halo;
     A.geo.wcx = g.wcx;
     A.geo.wcy = g.wcy;
     A.chunk = g.chunk;
@@ -315,16 +316,28 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
             PIC_TRY((bulk_attr<false, false>(sm)));
             push_kernel_bulk<false, false><<<grid, block, sm, h->stream>>>(A);
         }
+    } else if (h->cfg.push_variant == 3) {
+        // warp-summed deposit groups: measured 5% slower at 2048^2 x 32 ppc
+        // (1.144 vs 1.085 ms), so opt-in
+        const size_t sm = push_smem(g);
+        if (charged && dep)
+            push_kernel<true, true, true><<<grid, block, sm, h->stream>>>(A);
+        else if (charged)
+            push_kernel<true, false, false><<<grid, block, sm, h->stream>>>(A);
+        else if (dep)
+            push_kernel<false, true, true><<<grid, block, sm, h->stream>>>(A);
+        else
+            push_kernel<false, false, false><<<grid, block, sm, h->stream>>>(A);
     } else {
         const size_t sm = push_smem(g);
         if (charged && dep)
-            push_kernel<true, true><<<grid, block, sm, h->stream>>>(A);
+            push_kernel<true, true, false><<<grid, block, sm, h->stream>>>(A);
         else if (charged)
-            push_kernel<true, false><<<grid, block, sm, h->stream>>>(A);
+            push_kernel<true, false, false><<<grid, block, sm, h->stream>>>(A);
         else if (dep)
-            push_kernel<false, true><<<grid, block, sm, h->stream>>>(A);
+            push_kernel<false, true, false><<<grid, block, sm, h->stream>>>(A);
         else
-            push_kernel<false, false><<<grid, block, sm, h->stream>>>(A);
+            push_kernel<false, false, false><<<grid, block, sm, h->stream>>>(A);
     }
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;

@@ -48,7 +48,7 @@ struct PushGeo {
     const float *ex, *ey;
     unsigned long long *rho;
     DevState *dev;
-    int nx, ny, tw, th, halo, wcx, wcy;
+    int nx, ny, tw, th, hx, hy, wcx, wcy;  // window halo hx, hy; size wcx x wcy cells
     float qm_dt, dtdx, dtdy;
     unsigned long long qmul;  // q_int as two's complement
     double ke_scale, p_scale; // m/4, m/2 (0 disables the diagnostics)
@@ -90,7 +90,7 @@ __device__ __forceinline__ Window setup_window(const PushGeo &A, unsigned char *
     W.on = anc >= 0;
     W.wx0 = W.wy0 = 0;
     if (W.on) {
-        int wx0 = (anc & 0xFFFF) * A.tw - A.halo, wy0 = (anc >> 16) * A.th - A.halo;
+        int wx0 = (anc & 0xFFFF) * A.tw - A.hx, wy0 = (anc >> 16) * A.th - A.hy;
         wx0 %= A.nx;
         if (wx0 < 0) wx0 += A.nx;
         wy0 %= A.ny;
@@ -134,8 +134,44 @@ __device__ __forceinline__ void deposit_group(const PushGeo &A, const Window &W,
     }
 }
 
+// Sum of the lanes' (count, sum fx, sum fy, sum fx*fy) over each maximal run
+// of consecutive lanes with the same key; returns true on the run's first
+// lane, which holds the run's total.  All 32 lanes must call it (full-warp
+// shuffles and ballot); key -1 marks a lane without a group.  Runs are
+// exact for any key sequence: lane i adds the partial of lane i + o only
+// while i + o lies before the next run start, so no lane is counted twice.
+__device__ __forceinline__ bool warp_group_sum(int key, unsigned &c, unsigned &fx, unsigned &fy,
+                                               unsigned long long &xy)
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(full, key, 1);
+    const bool head = lane == 0 || key != prev;
+    const unsigned heads = __ballot_sync(full, head);
+    const unsigned after = heads & (0xfffffffeu << lane);  // run starts after this lane
+    const int seg_end = after ? __ffs(after) - 1 : 32;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned c2 = __shfl_down_sync(full, c, o);
+        const unsigned fx2 = __shfl_down_sync(full, fx, o);
+        const unsigned fy2 = __shfl_down_sync(full, fy, o);
+        const unsigned long long xy2 = __shfl_down_sync(full, xy, o);
+        if (lane + o < seg_end) {
+            c += c2;
+            fx += fx2;
+            fy += fy2;
+            xy += xy2;
+        }
+    }
+    return head;
+}
+
 // Gather, push and deposit four consecutive particles held in registers.
-template <bool GATHER, bool DEPOSIT>
+// AGG: the lanes' main groups are summed across the warp (warp_group_sum)
+// before the deposit, so that a warp whose particles share a cell issues
+// one set of atomics instead of 32 conflicting ones; every lane of the warp
+// must then call this function together.
+template <bool GATHER, bool DEPOSIT, bool AGG>
 __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int (&cc)[4],
                                           float (&xo)[4], float (&yo)[4], float (&xv)[4],
                                           float (&yv)[4], float &ke, float &px, float &py,
@@ -230,7 +266,12 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
             }
         }
     }
-    if (DEPOSIT && gcnt) deposit_group(A, W, gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+    if (DEPOSIT && AGG) {
+        if (warp_group_sum(gcnt ? gkey : -1, gcnt, gfx, gfy, gxy) && gcnt)
+            deposit_group(A, W, gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+    } else if (DEPOSIT && gcnt) {
+        deposit_group(A, W, gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+    }
 }
 
 __device__ __forceinline__ void store_quad(const PushArgs &A, long long q, const int (&cc)[4],
@@ -291,7 +332,9 @@ __device__ __forceinline__ void finish_block(const PushGeo &A, const Window &W, 
 
 // One push block: particles [base, end) of one run (end a multiple of 4 or
 // the end of the padded array), window anchored at tile `anc` (-1: none).
-template <bool GATHER, bool DEPOSIT>
+// Thread t owns the quads base + 4t + 4k blockDim.x; the loop runs while any
+// lane of the warp has a quad, so that the warp stays converged for AGG.
+template <bool GATHER, bool DEPOSIT, bool AGG>
 __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, unsigned char *smem,
                                            long long base, long long end, int anc)
 {
@@ -303,18 +346,28 @@ __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, 
 
     float ke = 0.f, px = 0.f, py = 0.f;
     bool bad = false;
-    for (long long q = base + 4ll * threadIdx.x; q < end; q += 4ll * blockDim.x) {
-        // plain (coherent) loads: with an in-place pass the same addresses are stored below
-        const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
-        const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
-        const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
-        const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
-        const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
-        int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-        float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
-        float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
-        push_quad<GATHER, DEPOSIT>(G, W, cc, xo, yo, xv, yv, ke, px, py, bad);
-        store_quad(A, q, cc, xo, yo, xv, yv);
+    const long long lane4 = 4ll * (threadIdx.x & 31);
+    for (long long qw = base + 4ll * (threadIdx.x & ~31u); qw < end; qw += 4ll * blockDim.x) {
+        const long long q = qw + lane4;
+        const bool live = q < end;
+        int cc[4] = {-1, -1, -1, -1};
+        float xo[4] = {0.f, 0.f, 0.f, 0.f}, yo[4] = {0.f, 0.f, 0.f, 0.f};
+        float xv[4] = {0.f, 0.f, 0.f, 0.f}, yv[4] = {0.f, 0.f, 0.f, 0.f};
+        if (live) {
+            // plain (coherent) loads: with an in-place pass the same addresses are stored below
+            const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
+            const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
+            const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
+            const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+            const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+            cc[0] = c4.x, cc[1] = c4.y, cc[2] = c4.z, cc[3] = c4.w;
+            xo[0] = a4.x, xo[1] = a4.y, xo[2] = a4.z, xo[3] = a4.w;
+            yo[0] = b4.x, yo[1] = b4.y, yo[2] = b4.z, yo[3] = b4.w;
+            xv[0] = u4.x, xv[1] = u4.y, xv[2] = u4.z, xv[3] = u4.w;
+            yv[0] = v4.x, yv[1] = v4.y, yv[2] = v4.z, yv[3] = v4.w;
+        }
+        push_quad<GATHER, DEPOSIT, AGG>(G, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+        if (live) store_quad(A, q, cc, xo, yo, xv, yv);
     }
     finish_block<DEPOSIT>(G, W, sAcc, ke, px, py, bad);
 }

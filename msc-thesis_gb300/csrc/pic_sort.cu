@@ -36,9 +36,10 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
     sort_hist_block(A, single_geo(A), S, base, n);
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 5) sort_scatter_kernel(SortArgs A)
+__global__ void __launch_bounds__(SORT_THREADS, 4) sort_scatter_kernel(SortArgs A)
 {
-    __shared__ SortSmem S;
+    extern __shared__ __align__(16) unsigned char smem[];
+    ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem);
     const long long n = *A.d_n;
     const long long base = (long long)blockIdx.x * SORT_CHUNK;
     if (base >= n) return;
@@ -185,6 +186,14 @@ __global__ void sort_anchor_kernel(SortArgs A, long long nchunks)
     A.anchor[b] = (t % A.ntx) | ((t / A.ntx) << 16);
 }
 
+// the scatter kernels use more than the default 48 KB of dynamic shared memory
+pic_status scatter_smem_attr(const void *kernel)
+{
+    PIC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)SCATTER_SMEM));
+    return PIC_OK;
+}
+
 // Sort species s from buffer 0 into buffer 1 and compute the chunk anchors.
 pic_status launch_sort(pic_handle *h, int s)
 {
@@ -232,7 +241,8 @@ pic_status launch_sort(pic_handle *h, int s)
     scan_add_kernel<<<grid_for(nkeys, 256), 256, 0, h->stream>>>(h->offset, h->cursor, nkeys,
                                                                h->bsum, &h->dev->n[s]);
     PIC_CUDA(cudaGetLastError());
-    sort_scatter_kernel<<<gp, SORT_THREADS, 0, h->stream>>>(A);
+    PIC_TRY(scatter_smem_attr((const void *)sort_scatter_kernel));
+    sort_scatter_kernel<<<gp, SORT_THREADS, SCATTER_SMEM, h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     sort_anchor_kernel<<<(unsigned)((B.nchunks + 255) / 256), 256, 0, h->stream>>>(A, B.nchunks);
     PIC_CUDA(cudaGetLastError());

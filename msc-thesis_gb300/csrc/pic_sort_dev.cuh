@@ -4,6 +4,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include "pic_internal.cuh"
 
 namespace pic {
@@ -209,80 +211,125 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
         if (S.hcnt[r]) atomicAdd(A.count + S.hkey[r], S.hcnt[r]);
 }
 
+// Shared memory of a scatter block: the counting state, each key's first
+// slot in a block-local staging order, and the global destination of every
+// staged particle.  Once the destinations are known, the staging buffers
+// (three fields at a time) alias the counting state.
+struct ScatterSmem {
+    SortSmem s;
+    uint32_t lbase[SORT_KEYS];
+    uint32_t hlbase[HASH_SLOTS];
+    uint32_t dst[SORT_CHUNK];
+    uint32_t total;
+};
+static_assert(offsetof(ScatterSmem, dst) >= 3 * SORT_CHUNK * sizeof(uint32_t),
+              "staging buffers must fit in the counting state");
+constexpr size_t SCATTER_SMEM = sizeof(ScatterSmem);
+
+// one staging phase: up to three 32-bit fields moved through shared memory
+// so that the global stores follow the destination order (consecutive
+// threads write consecutive slots of a key's slice)
+template <int NF>
+__device__ __forceinline__ void stage_fields(ScatterSmem &S, long long base, long long end,
+                                             const int (&lpos)[SORT_PER_THREAD],
+                                             const uint32_t *const (&src)[3], uint32_t *const (&dst)[3])
+{
+    uint32_t *stage = reinterpret_cast<uint32_t *>(&S);
+    __syncthreads();  // previous phase has left the staging buffers
+#pragma unroll
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
+        if (i < end && lpos[j] >= 0) {
+#pragma unroll
+            for (int f = 0; f < NF; ++f) stage[f * SORT_CHUNK + lpos[j]] = src[f][i];
+        }
+    }
+    __syncthreads();
+    const int total = (int)S.total;
+    for (int t = threadIdx.x; t < total; t += SORT_THREADS) {
+        const uint32_t d = S.dst[t];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) dst[f][d] = stage[f * SORT_CHUNK + t];
+    }
+}
+
 // Scatter of particles [base, end) (one sort block) to their sorted slots.
-__device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyGeo &G, SortSmem &S,
-                                                   long long base, long long end)
+// Each distinct key reserves its global slice (one global atomic per key and
+// block) and a block-local staging range; particles are staged in
+// shared memory in slice order and written out with consecutive threads on
+// consecutive slots.
+__device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyGeo &G,
+                                                   ScatterSmem &S, long long base, long long end)
 {
     const int k0 = window_start(A, G, base, end);
-    init_smem(S);
+    init_smem(S.s);
+    if (threadIdx.x == 0) S.total = 0u;
     __syncthreads();
     int keys[SORT_PER_THREAD];
-    count_keys(A, G, S, base, end, k0, keys);
+    count_keys(A, G, S.s, base, end, k0, keys);
     __syncthreads();
-    // reserve each distinct key's slice of the output once per block
+    // reserve each distinct key's slice of the output and of the staging order
     for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) {
-        const uint32_t v = S.cnt[r];
-        S.base[r] = (v && k0 + r < A.nkeys) ? atomicAdd(A.cursor + k0 + r, v) : 0u;
-        S.cnt[r] = 0u;
+        const uint32_t v = S.s.cnt[r];
+        const bool use = v && k0 + r < A.nkeys;
+        S.s.base[r] = use ? atomicAdd(A.cursor + k0 + r, v) : 0u;
+        S.lbase[r] = use ? atomicAdd(&S.total, v) : 0u;
+        S.s.cnt[r] = 0u;
     }
     for (int r = threadIdx.x; r < HASH_SLOTS; r += SORT_THREADS) {
-        const uint32_t v = S.hcnt[r];
-        S.hbase[r] = v ? atomicAdd(A.cursor + S.hkey[r], v) : 0u;
-        S.hcnt[r] = 0u;
+        const uint32_t v = S.s.hcnt[r];
+        S.s.hbase[r] = v ? atomicAdd(A.cursor + S.s.hkey[r], v) : 0u;
+        S.hlbase[r] = v ? atomicAdd(&S.total, v) : 0u;
+        S.s.hcnt[r] = 0u;
     }
     __syncthreads();
-    // destinations of this thread's particles: one reservation per run ...
+    // destination and staging slot of every particle: one reservation per run
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
         const int key = keys[j];
         const Run R = warp_run(key);
-        uint32_t d = 0;
+        uint32_t d = 0, l = 0;
         if (R.head && key >= 0) {
             if (key & FALLBACK_BIT) {
                 d = atomicAdd(A.cursor + (key & ~FALLBACK_BIT), (uint32_t)R.len);
+                l = atomicAdd(&S.total, (uint32_t)R.len);
             } else if ((unsigned)(key - k0) < (unsigned)SORT_KEYS) {
                 const int r = key - k0;
-                d = S.base[r] + atomicAdd(S.cnt + r, (uint32_t)R.len);
+                const uint32_t o = atomicAdd(S.s.cnt + r, (uint32_t)R.len);
+                d = S.s.base[r] + o;
+                l = S.lbase[r] + o;
             } else {
-                const int slot = hash_find(S.hkey, key);  // counted in the table in pass 1
-                d = S.hbase[slot] + atomicAdd(S.hcnt + slot, (uint32_t)R.len);
+                const int slot = hash_find(S.s.hkey, key);  // counted in the table in pass 1
+                const uint32_t o = atomicAdd(S.s.hcnt + slot, (uint32_t)R.len);
+                d = S.s.hbase[slot] + o;
+                l = S.hlbase[slot] + o;
             }
         }
         d = __shfl_sync(0xffffffffu, d, R.hidx) + (uint32_t)R.rank;
-        keys[j] = key >= 0 ? (int)d : -1;  // n < 2^31
+        l = __shfl_sync(0xffffffffu, l, R.hidx) + (uint32_t)R.rank;
+        if (key >= 0) S.dst[l] = d;
+        keys[j] = key >= 0 ? (int)l : -1;
     }
-    // ... then the copies, four particles at a time with their loads first
-#pragma unroll
-    for (int g = 0; g < SORT_PER_THREAD; g += 4) {
-        int c[4];
-        uint32_t p[4];
-        float a[4], b[4], u[4], v[4], z[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const long long i = base + (long long)(g + t) * SORT_THREADS + threadIdx.x;
-            if (i < end) {
-                c[t] = A.cin[i];
-                a[t] = A.oxin[i];
-                b[t] = A.oyin[i];
-                u[t] = A.vxin[i];
-                v[t] = A.vyin[i];
-                p[t] = A.pidin[i];
-                z[t] = A.vzin ? A.vzin[i] : 0.f;
-            }
-        }
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const long long i = base + (long long)(g + t) * SORT_THREADS + threadIdx.x;
-            if (i >= end || keys[g + t] < 0) continue;
-            const long long d = keys[g + t];
-            A.cout[d] = c[t];
-            A.oxout[d] = a[t];
-            A.oyout[d] = b[t];
-            A.vxout[d] = u[t];
-            A.vyout[d] = v[t];
-            A.pidout[d] = p[t];
-            if (A.vzin) A.vzout[d] = z[t];
-        }
+    {
+        const uint32_t *const src[3] = {reinterpret_cast<const uint32_t *>(A.cin),
+                                        reinterpret_cast<const uint32_t *>(A.oxin),
+                                        reinterpret_cast<const uint32_t *>(A.oyin)};
+        uint32_t *const dst[3] = {reinterpret_cast<uint32_t *>(A.cout),
+                                  reinterpret_cast<uint32_t *>(A.oxout),
+                                  reinterpret_cast<uint32_t *>(A.oyout)};
+        stage_fields<3>(S, base, end, keys, src, dst);
+    }
+    {
+        const uint32_t *const src[3] = {reinterpret_cast<const uint32_t *>(A.vxin),
+                                        reinterpret_cast<const uint32_t *>(A.vyin), A.pidin};
+        uint32_t *const dst[3] = {reinterpret_cast<uint32_t *>(A.vxout),
+                                  reinterpret_cast<uint32_t *>(A.vyout), A.pidout};
+        stage_fields<3>(S, base, end, keys, src, dst);
+    }
+    if (A.vzin) {
+        const uint32_t *const src[3] = {reinterpret_cast<const uint32_t *>(A.vzin), nullptr, nullptr};
+        uint32_t *const dst[3] = {reinterpret_cast<uint32_t *>(A.vzout), nullptr, nullptr};
+        stage_fields<1>(S, base, end, keys, src, dst);
     }
 }
 

@@ -78,7 +78,7 @@ extern "C" pic_status pic_autotune(pic_config *cfg, int species, const pic_init_
             best_th = th;
         }
     }
-    const int cadences[] = {10, 20, 40, 80};
+    const int cadences[] = {2, 5, 10, 20, 40, 80};
     base = best;
     for (int se : cadences) {
         if (se == base.sort_every) continue;

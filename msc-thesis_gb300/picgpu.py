@@ -155,6 +155,7 @@ SIGNATURES = {
     "pic_ensemble_diagnostics": [_H, C.c_int, C.POINTER(Diag)],
     "pic_ensemble_get_history": [_H, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp],
     "pic_ensemble_get_particles": [_H, C.c_int, C.POINTER(C.c_longlong), _vp, _vp, _vp, _vp],
+    "pic_ensemble_autotune": [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p],
     "pic_run_host": [_H, C.c_longlong, _vp, _vp, _vp, _vp, C.c_longlong, C.c_int,
                      _vp, _vp, _vp, _vp],
     "pic_diagnostics": [_H, C.POINTER(Diag)],
@@ -487,6 +488,18 @@ class Handle:
         out = np.empty((self.cfg.ny, self.cfg.nx), np.int64)
         self._c("pic_get_rho_fixed", _ptr(out))
         return out
+
+
+def ensemble_autotune(cfgs, specs, trial_steps: int = 20) -> TuneResult:
+    """Pick chunk and sort cadence for an ensemble (pic_ensemble_autotune); the
+    chosen values are written into cfgs[0]."""
+    arr = (Config * len(cfgs))(*cfgs)
+    sp = (InitSpec * len(specs))(*specs)
+    r = TuneResult()
+    _check(load().pic_ensemble_autotune(C.addressof(arr), len(cfgs), C.addressof(sp), trial_steps,
+                                        C.addressof(r)), "pic_ensemble_autotune")
+    cfgs[0].chunk, cfgs[0].sort_every = arr[0].chunk, arr[0].sort_every
+    return r
 
 
 class Ensemble:
