@@ -290,6 +290,19 @@ def bench_ensemble(args):
             h.synchronize()
             plain_ms += a0.elapsed_time(a1)
     plain_value = total * args.steps / (plain_ms / 1000.0) if plain_ms else None
+    # forward + adjoint of every run (checkpoint every `every` steps, reversal
+    # in between): particle-steps of the forward over the whole call's time
+    adj = None
+    if args.adjoint_steps:
+        with P.Ensemble(cfgs) as E:
+            E.adjoint(specs, 2 * args.every, args.every, gradients=False)  # warm-up (plans)
+            t0 = time.perf_counter()
+            res, _ = E.adjoint(specs, args.adjoint_steps, args.every, gradients=False)
+            el = time.perf_counter() - t0
+        adj = {"value": total * args.adjoint_steps / el, "unit": "particle-steps/s",
+               "steps": args.adjoint_steps, "every": args.every, "seconds": el,
+               "note": "forward with checkpoints + reversed backward walk, one call",
+               "J_run0": res[0][0], "dJ_dbeam_run0": res[0][1], "dJ_damp_run0": res[0][2]}
     cells = int(sum(int(g) * int(g) for g in grids))
     step_bytes = BYTES_PER_PARTICLE * total + BYTES_PER_CELL * cells
     achieved = step_bytes * args.steps / (ms / 1000.0) / 1e9
@@ -308,6 +321,7 @@ def bench_ensemble(args):
                              "ms_per_step": plain_ms / args.steps,
                              "tuned": {f"{k[0]}^2x{k[1]}": v for k, v in tuned.items()}},
         "speedup_vs_plain": ens_value / plain_value if plain_value else None,
+        "batched_adjoint": adj,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "kernel": "whole ensemble step"},
         "cpu_baseline": None, "e2e": None,
@@ -329,6 +343,9 @@ def main():
     ap.add_argument("--sort-every", type=int, default=SORT_EVERY)
     ap.add_argument("--push-variant", type=int, default=0, help="0 auto, 1 direct, 2 bulk copy")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (untimed setup)")
+    ap.add_argument("--adjoint-steps", type=int, default=500,
+                    help="ensemble workload: steps of the timed forward+adjoint (0: skip)")
+    ap.add_argument("--every", type=int, default=50, help="adjoint checkpoint spacing")
     ap.add_argument("--no-plain", action="store_true",
                     help="ensemble workload: skip the one-run-at-a-time comparison")
     ap.add_argument("--workload", default="landau", choices=["landau", "ensemble"],

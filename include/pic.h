@@ -407,6 +407,24 @@ pic_status pic_ensemble_get_history(pic_ensemble *e, int run, int which, long lo
                                     long long count, double *out);
 pic_status pic_ensemble_get_particles(pic_ensemble *e, int run, long long *n, double *x, double *y,
                                       double *vx, double *vy);
+/* Discrete adjoint of every run of the ensemble (see pic_adjoint_run): each
+ * run is loaded from specs[r], primed and stepped nsteps times, and the
+ * gradients of its final field energy J_r with respect to its initial state
+ * are computed.  Memory: instead of a ring of recomputed positions, each
+ * segment of `every` steps is walked backwards by reversing the leapfrog
+ * (x -= dt v, field of the reversed positions, v -= dt (q/m) F) from an
+ * exact checkpoint of its end state, so the ensemble keeps one checkpoint
+ * (24 bytes per particle slot) per segment and no per-step storage;
+ * checkpoints go to pinned host memory when device memory runs out.  The
+ * adjoint arrays travel with the particles through the sorts.  out[r]
+ * (nruns entries) receives J_r, dJ_r/d(beam_v) and dJ_r/d(pert_amp) of
+ * specs[r]; gradient arrays (may be NULL) are the runs' arrays in run order,
+ * each in particle-id order (run r starts after the particles of runs
+ * 0..r-1).  Leaves the ensemble at step nsteps.  No counterpart in the
+ * reference. */
+pic_status pic_ensemble_adjoint(pic_ensemble *e, const pic_init_spec *specs, long long nsteps,
+                                int every, double *dJ_dx0, double *dJ_dy0, double *dJ_dvx0,
+                                double *dJ_dvy0, pic_adjoint_result *out);
 /* Pick the push chunk (and with it every run's sort tile) and the sort
  * cadence of an ensemble by timing short runs of it, as pic_autotune does
  * for one handle: chunk from (2048, 4096, 8192, 16384), then cadence from

@@ -21,7 +21,7 @@
 #include <algorithm>
 #include <vector>
 
-#include "pic_internal.cuh"
+#include "pic_adjoint_dev.cuh"
 
 namespace pic {
 
@@ -39,36 +39,6 @@ struct AdjArgs {
     float drift_dt;            // dt for the drift adjoint (0: none)
     float q_over_dA;
 };
-
-struct Cic {
-    int i00, i10, i01, i11;
-    float fx, fy;
-    bool ok;
-};
-
-__device__ __forceinline__ Cic cic_of(int c, float ox, float oy, int nx, int ny)
-{
-    Cic w;
-    const int cx = c & 0xFFFF, cy = c >> 16;
-    w.ok = c >= 0 && cx < nx && cy < ny;
-    const int cx1 = (cx + 1 == nx) ? 0 : cx + 1, cy1 = (cy + 1 == ny) ? 0 : cy + 1;
-    w.i00 = cy * nx + cx;
-    w.i10 = cy * nx + cx1;
-    w.i01 = cy1 * nx + cx;
-    w.i11 = cy1 * nx + cx1;
-    w.fx = ox;
-    w.fy = oy;
-    return w;
-}
-
-// sum_k grad w_k s_k, physical units
-__device__ __forceinline__ float2 grad_dot(const Cic &w, float s00, float s10, float s01,
-                                           float s11, float inv_dx, float inv_dy)
-{
-    const float fx = w.fx, fy = w.fy;
-    return make_float2(((1.f - fy) * (s10 - s00) + fy * (s11 - s01)) * inv_dx,
-                       ((1.f - fx) * (s01 - s00) + fx * (s11 - s10)) * inv_dy);
-}
 
 // drift adjoint, kick local term and scatter of mu
 __global__ void __launch_bounds__(256) adj_kick_scatter_kernel(AdjArgs A)
@@ -124,18 +94,10 @@ __global__ void __launch_bounds__(256) adj_kspace_kernel(const float2 *gh, float
                                                          int nh, float kx1, float ky1, float inv_eps0_n)
 {
     const long long total = (long long)ny * nh;
-    const bool nx_even = (nx & 1) == 0, ny_even = (ny & 1) == 0;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
         const int my = (int)(idx / nh), mx = (int)(idx - (long long)my * nh);
-        const int sy = (2 * my <= ny) ? my : my - ny;
-        const float kx = kx1 * (float)mx, ky = ky1 * (float)sy;
-        const float kxe = (nx_even && 2 * mx == nx) ? 0.f : kx;
-        const float kye = (ny_even && 2 * my == ny) ? 0.f : ky;
-        const float2 a = gh[idx], b = gh[total + idx];
-        const float hr = kxe * a.x + kye * b.x, hi = kxe * a.y + kye * b.y;
-        const float inv = (idx == 0) ? 0.f : inv_eps0_n / (kx * kx + ky * ky);
-        ph[idx] = make_float2(-hi * inv, hr * inv);  // i (hr + i hi)
+        ph[idx] = adj_mode(gh[idx], gh[total + idx], mx, my, nx, ny, kx1, ky1, inv_eps0_n, idx == 0);
     }
 }
 
@@ -407,7 +369,7 @@ pic_status adjoint_run(pic_handle *h, const pic_init_spec *spec, long long nstep
         if (spec) {
             double sb = 0.0;
             for (long long i = 0; i < n; ++i) sb += (i & 1) ? -hb[2 * n + i] : hb[2 * n + i];
-            out->dJ_dbeam_v = spec->beam_v != 0.0 ? sb : 0.0;
+            out->dJ_dbeam_v = sb;  // vx carries +-beam_v by id parity
             std::vector<double> dA(2 * (size_t)n);
             double *dAd;
             PIC_TRY(W.alloc(&dAd, 2 * (size_t)n));

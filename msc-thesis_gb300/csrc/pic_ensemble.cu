@@ -28,31 +28,12 @@
 #include <numeric>
 #include <vector>
 
+#include "pic_ensemble.cuh"
 #include "pic_field_dev.cuh"
 #include "pic_push_dev.cuh"
-#include "pic_sort_dev.cuh"
 
 namespace pic {
 
-struct EnsRun {
-    int nx, ny, nh, tw, th, ntx, nty, wcx, wcy, hx, hy;
-    int key_off;
-    long long n, cap4, poff, goff, ncp, khoff, nk;
-    float qm_dt, dtdx, dtdy, rho_scale;
-    float kx1, ky1, inv_eps0_n;
-    unsigned long long qmul;
-    double ke_scale, p_scale, fe_scale;
-    long long mean_fix;
-    double dx, dy;
-};
-
-struct SegBlock {
-    long long base;
-    int count;
-    int run;
-};
-
-constexpr int ENS_NODES_PER_BLOCK = 2048;
 
 // ------------------------------------------------------------------ kernels
 template <bool GATHER, bool DEPOSIT>
@@ -202,53 +183,7 @@ __global__ void ens_advance_kernel(DevState *devs, double *hist, int cap, int ki
 // ------------------------------------------------------------------ host side
 using namespace pic;
 
-struct pic_ensemble {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int nruns = 0;
-    std::vector<pic_config> cfg;     // caller order
-    std::vector<int> slot_of, run_of;
-    std::vector<EnsRun> runs;        // slot order
-    EnsRun *d_runs = nullptr;
-    long long nslots = 0, nnodes = 0, nmodes = 0, nkeys = 0;
-    int chunk = 8192, halo = 2, sort_every = 20, hist_cap = 4096;
-    // particles, two buffers
-    int32_t *cell[2] = {nullptr, nullptr};
-    float *ox[2] = {nullptr, nullptr}, *oy[2] = {nullptr, nullptr};
-    float *vx[2] = {nullptr, nullptr}, *vy[2] = {nullptr, nullptr};
-    uint32_t *pid[2] = {nullptr, nullptr};
-    // grids
-    unsigned long long *rho_fix = nullptr;
-    float *rho = nullptr, *e = nullptr;
-    float2 *rhohat = nullptr, *ehat = nullptr;
-    // sort
-    uint32_t *count = nullptr, *offset = nullptr, *cursor = nullptr;
-    uint32_t *bsum = nullptr, *bsum_s = nullptr, *bsum2 = nullptr;
-    long long *d_total = nullptr;
-    // work tables
-    SegBlock *push_blk = nullptr, *sort_blk = nullptr, *node_blk = nullptr, *mode_blk = nullptr;
-    int npush = 0, nsort = 0, nnode_blk = 0, nmode_blk = 0;
-    int32_t *anchor = nullptr;
-    size_t push_smem = 0;
-    // diagnostics
-    DevState *dev = nullptr;
-    double *hist = nullptr;
-    // FFT groups: runs of one grid size, adjacent slots
-    struct Group {
-        int nx, ny, first, count;
-        cufftHandle r2c = 0, c2r = 0;
-    };
-    std::vector<Group> groups;
-    // graphs
-    cudaGraphExec_t g_one = nullptr, g_period = nullptr, g_sortstep = nullptr;
-    int since_sort = 0;
-    bool ready = false;
-    // export staging
-    double *stage = nullptr;
-    size_t stage_n = 0;
-};
-
-namespace {
+namespace pic {
 
 pic_status ens_bad(const std::string &m)
 {
@@ -276,19 +211,14 @@ void ens_free(pic_ensemble *E)
     for (auto &G : E->groups) {
         if (G.r2c) cufftDestroy(G.r2c);
         if (G.c2r) cufftDestroy(G.c2r);
+        if (G.r2c2) cufftDestroy(G.r2c2);
+        if (G.c2r1) cufftDestroy(G.c2r1);
     }
     if (E->g_one) cudaGraphExecDestroy(E->g_one);
     if (E->g_period) cudaGraphExecDestroy(E->g_period);
     if (E->g_sortstep) cudaGraphExecDestroy(E->g_sortstep);
     if (E->stream) cudaStreamDestroy(E->stream);
     delete E;
-}
-
-template <class T> pic_status ens_alloc(T **p, size_t n)
-{
-    *p = nullptr;
-    PIC_CUDA(cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T)));
-    return PIC_OK;
 }
 
 template <class T> pic_status upload(T **d, const std::vector<T> &h)
@@ -359,6 +289,11 @@ pic_status ens_layout(pic_ensemble *E)
         R.ky1 = (float)(2.0 * 3.14159265358979323846 / c.Ly);
         R.inv_eps0_n = (float)(1.0 / (c.eps0 * (double)c.nx * (double)c.ny));
         R.qmul = (unsigned long long)(long long)D.q_int;
+        R.dt = (float)c.dt;
+        R.inv_dx = (float)(1.0 / R.dx);
+        R.inv_dy = (float)(1.0 / R.dy);
+        R.q_dA = (float)(D.q / (R.dx * R.dy));
+        R.eps0_dA = (float)(c.eps0 * R.dx * R.dy);
         R.ke_scale = 0.25 * D.m;
         R.p_scale = 0.5 * D.m;
         R.fe_scale = 0.5 * c.eps0 * R.dx * R.dy * (double)c.nx * (double)c.ny;
@@ -489,8 +424,6 @@ PushArgs ens_push_args(pic_ensemble *E, int src)
     return A;
 }
 
-// kind: 0 step (gather, drift, deposit), 1 prime (kick -1/2, no drift, no
-// deposit), 2 deposit only (no gather, no drift)
 pic_status ens_launch_push(pic_ensemble *E, int src, int kind)
 {
     if (!E->npush) return PIC_OK;
@@ -502,8 +435,10 @@ pic_status ens_launch_push(pic_ensemble *E, int src, int kind)
         ens_push_kernel<true, true><<<grid, block, sm, st>>>(A, E->push_blk, E->d_runs, E->anchor, 1.f, 1.f);
     else if (kind == 1)
         ens_push_kernel<true, false><<<grid, block, sm, st>>>(A, E->push_blk, E->d_runs, E->anchor, -0.5f, 0.f);
-    else
+    else if (kind == 2)
         ens_push_kernel<false, true><<<grid, block, sm, st>>>(A, E->push_blk, E->d_runs, E->anchor, 0.f, 0.f);
+    else
+        ens_push_kernel<false, true><<<grid, block, sm, st>>>(A, E->push_blk, E->d_runs, E->anchor, 0.f, -1.f);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }
@@ -535,7 +470,7 @@ pic_status ens_poisson(pic_ensemble *E)
     return ens_advance(E, ADV_FIELD);
 }
 
-SortArgs ens_sort_args(pic_ensemble *E)
+SortArgs ens_sort_args(pic_ensemble *E, const float *const *xin, float *const *xout)
 {
     SortArgs A;
     memset(&A, 0, sizeof A);
@@ -557,14 +492,18 @@ SortArgs ens_sort_args(pic_ensemble *E)
     A.cursor = E->cursor;
     A.nkeys = E->nkeys;
     A.err = &E->dev[0].err;
+    for (int k = 0; k < 4; ++k) {
+        A.xin[k] = xin ? reinterpret_cast<const uint32_t *>(xin[k]) : nullptr;
+        A.xout[k] = xout ? reinterpret_cast<uint32_t *>(xout[k]) : nullptr;
+    }
     return A;
 }
 
 // sort every run from buffer 0 into buffer 1; push-block anchors
-pic_status ens_sort(pic_ensemble *E)
+pic_status ens_sort(pic_ensemble *E, const float *const *xin, float *const *xout)
 {
     cudaStream_t st = E->stream;
-    const SortArgs A = ens_sort_args(E);
+    const SortArgs A = ens_sort_args(E, xin, xout);
     PIC_CUDA(cudaMemsetAsync(E->count, 0, sizeof(uint32_t) * (size_t)E->nkeys, st));
     ens_sort_hist_kernel<<<E->nsort, SORT_THREADS, 0, st>>>(A, E->sort_blk, E->d_runs);
     PIC_CUDA(cudaGetLastError());
@@ -625,7 +564,7 @@ pic_status ens_graphs(pic_ensemble *E)
     return PIC_OK;
 }
 
-pic_status ens_need(pic_ensemble *E, int run = -1)
+pic_status ens_need(pic_ensemble *E, int run)
 {
     if (!E) {
         set_error("null ensemble");
@@ -639,7 +578,7 @@ pic_status ens_need(pic_ensemble *E, int run = -1)
     return PIC_OK;
 }
 
-}  // namespace
+}  // namespace pic
 
 // ------------------------------------------------------------------ C ABI
 extern "C" {
@@ -738,7 +677,7 @@ pic_status pic_ensemble_destroy(pic_ensemble *e)
 
 pic_status pic_ensemble_get_stream(pic_ensemble *e, void **stream)
 {
-    PIC_TRY(ens_need(e));
+    PIC_TRY(ens_need(e, -1));
     if (!stream) return PIC_ERR_INVALID_ARG;
     *stream = (void *)e->stream;
     return PIC_OK;
@@ -746,7 +685,7 @@ pic_status pic_ensemble_get_stream(pic_ensemble *e, void **stream)
 
 pic_status pic_ensemble_synchronize(pic_ensemble *e)
 {
-    PIC_TRY(ens_need(e));
+    PIC_TRY(ens_need(e, -1));
     PIC_CUDA(cudaStreamSynchronize(e->stream));
     unsigned err = 0;
     for (int r = 0; r < e->nruns; ++r) {
@@ -767,7 +706,7 @@ pic_status pic_ensemble_synchronize(pic_ensemble *e)
 
 pic_status pic_ensemble_init(pic_ensemble *e, const pic_init_spec *specs)
 {
-    PIC_TRY(ens_need(e));
+    PIC_TRY(ens_need(e, -1));
     if (!specs) return PIC_ERR_INVALID_ARG;
     std::vector<long long> n_slot(e->nruns);
     std::vector<int> lx(e->nruns, 0), ly(e->nruns, 0);
@@ -829,7 +768,7 @@ pic_status pic_ensemble_init(pic_ensemble *e, const pic_init_spec *specs)
 
 pic_status pic_ensemble_step(pic_ensemble *e, long long nsteps)
 {
-    PIC_TRY(ens_need(e));
+    PIC_TRY(ens_need(e, -1));
     if (nsteps < 0) return PIC_ERR_INVALID_ARG;
     if (!e->ready) {
         set_error("pic_ensemble_step: call pic_ensemble_init first");

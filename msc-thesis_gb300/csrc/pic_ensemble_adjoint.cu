@@ -1,0 +1,577 @@
+// pic_ensemble_adjoint.cu -- discrete adjoint of every run of an ensemble.
+//
+// The map and its transpose are those of pic_adjoint.cu (priming half kick,
+// leapfrog steps, J = final field energy per run).  What differs is how the
+// positions and fields of past steps are recovered.  The single-run adjoint
+// recomputes each segment forward into a ring; an ensemble holds too many
+// particles for that, so each segment is walked backwards by reversing the
+// leapfrog from an exact checkpoint of the segment's end state:
+//   x_s = x_(s+1) - dt v_(s+1/2)            (push pass with drift -1 + deposit)
+//   E(x_s)                                  (the ordinary field solve)
+//   v_(s-1/2) = v_(s+1/2) - dt (q/m) F(x_s) (fused into the adjoint kick)
+// The reversal is exact up to one rounding per step, and every segment
+// restarts from its checkpoint, so the error does not accumulate beyond
+// `every` steps.  Per backward step and run:
+//   kick      a_v += dt a_x; mu = dt (q/m) a_v; g = sum_i w(x_i) mu_i (shared-
+//             memory window as in the push); a_x += local CIC-gradient term
+//   solve     psi = S^T g: batched R2C of (gx, gy), k-space kernel, batched C2R
+//   gather    a_x += (q / dA) sum_m psi_m grad w_m(x)
+// The adjoint arrays move with the particles through the sorts of the
+// backward walk; at a checkpoint restore they are permuted into the
+// checkpoint's storage order through particle ids.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "pic_adjoint_dev.cuh"
+#include "pic_ensemble.cuh"
+#include "pic_push_dev.cuh"
+
+namespace pic {
+
+struct EnsAdjArgs {
+    const int32_t *cell;
+    const float *ox, *oy;
+    float *vx, *vy;            // un-kicked in place by the reversal
+    const float *e;            // field pool
+    float *ax, *ay, *avx, *avy;
+    float *g;                  // scatter planes: run r's gx at 2 goff, gy ncp later
+    const float *psi;          // S^T g: run r's plane at goff
+};
+
+struct Quad4 {
+    float *a[4];
+};
+struct CQuad4 {
+    const float *a[4];
+};
+
+__device__ __forceinline__ PushGeo adj_geo(const EnsRun &R, const float *e)
+{
+    PushGeo G = {};
+    G.ex = e + 2 * R.goff;
+    G.ey = G.ex + R.ncp;
+    G.nx = R.nx;
+    G.ny = R.ny;
+    G.tw = R.tw;
+    G.th = R.th;
+    G.hx = R.hx;
+    G.hy = R.hy;
+    G.wcx = R.wcx;
+    G.wcy = R.wcy;
+    return G;
+}
+
+// Drift adjoint, kick transpose (scatter of mu and local term) and, with
+// UNKICK, the reversal of the kick.  One push block of particles per CTA;
+// E and the scatter accumulators of the block's window live in shared
+// memory (the push window layout, accumulators as floats).
+template <bool UNKICK>
+__global__ void __launch_bounds__(256)
+ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs,
+                    const int32_t *__restrict__ anchor, float cscale, float dscale)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const SegBlock b = blk[blockIdx.x];
+    const EnsRun &R = runs[b.run];
+    const PushGeo G = adj_geo(R, A.e);
+    const Window W = setup_window(G, smem, anchor[blockIdx.x]);
+    load_window<true, true>(G, W);  // E into sE, accumulators zeroed
+    __syncthreads();
+    float *sgx = reinterpret_cast<float *>(W.sLo), *sgy = reinterpret_cast<float *>(W.sHi);
+    float *ggx = A.g + 2 * R.goff, *ggy = ggx + R.ncp;
+    const float qmdt = R.qm_dt, muc = cscale * R.qm_dt, ddt = dscale * R.dt;
+    const int nx = R.nx, ny = R.ny;
+    const long long end = b.base + b.count;
+    for (long long i = b.base + threadIdx.x; i < end; i += blockDim.x) {
+        const int c = A.cell[i];
+        const int cx = c & 0xFFFF, cy = c >> 16;
+        if (c < 0 || cx >= nx || cy >= ny) continue;
+        const float ox = A.ox[i], oy = A.oy[i];
+        const float ax = A.ax[i], ay = A.ay[i];
+        const float avx = fmaf(ddt, ax, A.avx[i]), avy = fmaf(ddt, ay, A.avy[i]);
+        const float mx = muc * avx, my = muc * avy;
+        const float gx = 1.f - ox, gy = 1.f - oy;
+        const float w00 = gx * gy, w10 = ox * gy, w01 = gx * oy, w11 = ox * oy;
+        float2 e00, e10, e01, e11;
+        int dxl = cx - W.wx0, dyl = cy - W.wy0;
+        if (dxl < 0) dxl += nx;
+        if (dyl < 0) dyl += ny;
+        if (W.on && dxl < G.wcx && dyl < G.wcy) {
+            const int l = dyl * W.nwx + dxl;
+            e00 = W.sE[l];
+            e10 = W.sE[l + 1];
+            e01 = W.sE[l + W.nwx];
+            e11 = W.sE[l + W.nwx + 1];
+            atomicAdd(sgx + l, w00 * mx);
+            atomicAdd(sgy + l, w00 * my);
+            atomicAdd(sgx + l + 1, w10 * mx);
+            atomicAdd(sgy + l + 1, w10 * my);
+            atomicAdd(sgx + l + W.nwx, w01 * mx);
+            atomicAdd(sgy + l + W.nwx, w01 * my);
+            atomicAdd(sgx + l + W.nwx + 1, w11 * mx);
+            atomicAdd(sgy + l + W.nwx + 1, w11 * my);
+        } else {
+            const Cic w = cic_of(c, ox, oy, nx, ny);
+            e00 = make_float2(G.ex[w.i00], G.ey[w.i00]);
+            e10 = make_float2(G.ex[w.i10], G.ey[w.i10]);
+            e01 = make_float2(G.ex[w.i01], G.ey[w.i01]);
+            e11 = make_float2(G.ex[w.i11], G.ey[w.i11]);
+            atomicAdd(ggx + w.i00, w00 * mx);
+            atomicAdd(ggy + w.i00, w00 * my);
+            atomicAdd(ggx + w.i10, w10 * mx);
+            atomicAdd(ggy + w.i10, w10 * my);
+            atomicAdd(ggx + w.i01, w01 * mx);
+            atomicAdd(ggy + w.i01, w01 * my);
+            atomicAdd(ggx + w.i11, w11 * mx);
+            atomicAdd(ggy + w.i11, w11 * my);
+        }
+        const float s00 = e00.x * mx + e00.y * my, s10 = e10.x * mx + e10.y * my;
+        const float s01 = e01.x * mx + e01.y * my, s11 = e11.x * mx + e11.y * my;
+        A.ax[i] = ax + (gy * (s10 - s00) + oy * (s11 - s01)) * R.inv_dx;
+        A.ay[i] = ay + (gx * (s01 - s00) + ox * (s11 - s10)) * R.inv_dy;
+        A.avx[i] = avx;
+        A.avy[i] = avy;
+        if (UNKICK) {  // the push's gather, then the kick taken back
+            const float Ex = gy * fmaf(gx, e00.x, ox * e10.x) + oy * fmaf(gx, e01.x, ox * e11.x);
+            const float Ey = gy * fmaf(gx, e00.y, ox * e10.y) + oy * fmaf(gx, e01.y, ox * e11.y);
+            A.vx[i] = fmaf(-qmdt, Ex, A.vx[i]);
+            A.vy[i] = fmaf(-qmdt, Ey, A.vy[i]);
+        }
+    }
+    __syncthreads();
+    if (W.on) {
+        for (int k = threadIdx.x; k < W.nw; k += blockDim.x) {
+            const float vx = sgx[k], vy = sgy[k];
+            if (vx != 0.f || vy != 0.f) {
+                const int a = k % W.nwx, bb = k / W.nwx;
+                const int gxn = (W.wx0 + a) % nx, gyn = (W.wy0 + bb) % ny;
+                const long long node = (long long)gyn * nx + gxn;
+                atomicAdd(ggx + node, vx);
+                atomicAdd(ggy + node, vy);
+            }
+        }
+    }
+}
+
+// adjoint of the deposit: a_x += (q/dA) sum_m psi_m grad w_m
+__global__ void __launch_bounds__(256)
+ens_adj_gather_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
+{
+    const SegBlock b = blk[blockIdx.x];
+    const EnsRun &R = runs[b.run];
+    const float *psi = A.psi + R.goff;
+    const long long end = b.base + b.count;
+    for (long long i = b.base + threadIdx.x; i < end; i += blockDim.x) {
+        const Cic w = cic_of(A.cell[i], A.ox[i], A.oy[i], R.nx, R.ny);
+        if (!w.ok) continue;
+        const float2 g = grad_dot(w, psi[w.i00], psi[w.i10], psi[w.i01], psi[w.i11], R.inv_dx,
+                                  R.inv_dy);
+        A.ax[i] = fmaf(R.q_dA, g.x, A.ax[i]);
+        A.ay[i] = fmaf(R.q_dA, g.y, A.ay[i]);
+    }
+}
+
+// psi^ of every run (into the first half of its spectrum pair)
+__global__ void __launch_bounds__(256)
+ens_adj_kspace_kernel(const float2 *__restrict__ ghat, float2 *__restrict__ psihat,
+                      const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
+{
+    const SegBlock b = blk[blockIdx.x];
+    const EnsRun &R = runs[b.run];
+    for (long long j = threadIdx.x; j < b.count; j += blockDim.x) {
+        const long long idx = b.base + j;
+        const int my = (int)(idx / R.nh), mx = (int)(idx - (long long)my * R.nh);
+        psihat[R.khoff + idx] = adj_mode(ghat[R.khoff + idx], ghat[R.khoff + R.nk + idx], mx, my,
+                                         R.nx, R.ny, R.kx1, R.ky1, R.inv_eps0_n, idx == 0);
+    }
+}
+
+// terminal condition: g = eps0 dA E
+__global__ void ens_adj_terminal_kernel(const float *__restrict__ e, float *__restrict__ g,
+                                        const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
+{
+    const SegBlock b = blk[blockIdx.x];
+    const EnsRun &R = runs[b.run];
+    for (long long j = threadIdx.x; j < b.count; j += blockDim.x) {
+        const long long node = b.base + j;
+        g[2 * R.goff + node] = R.eps0_dA * e[2 * R.goff + node];
+        g[2 * R.goff + R.ncp + node] = R.eps0_dA * e[2 * R.goff + R.ncp + node];
+    }
+}
+
+// storage order -> id order (per run, at poff + pid) and back
+__global__ void ens_to_id_kernel(const int32_t *__restrict__ cell, const uint32_t *__restrict__ pid,
+                                 CQuad4 in, Quad4 out, const SegBlock *__restrict__ blk,
+                                 const EnsRun *__restrict__ runs)
+{
+    const SegBlock b = blk[blockIdx.x];
+    const EnsRun &R = runs[b.run];
+    const long long end = b.base + b.count;
+    for (long long i = b.base + threadIdx.x; i < end; i += blockDim.x) {
+        const uint32_t p = pid[i];
+        if (cell[i] < 0 || (long long)p >= R.n) continue;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) out.a[k][R.poff + p] = in.a[k][i];
+    }
+}
+
+__global__ void ens_from_id_kernel(const int32_t *__restrict__ cell, const uint32_t *__restrict__ pid,
+                                   CQuad4 in, Quad4 out, const SegBlock *__restrict__ blk,
+                                   const EnsRun *__restrict__ runs)
+{
+    const SegBlock b = blk[blockIdx.x];
+    const EnsRun &R = runs[b.run];
+    const long long end = b.base + b.count;
+    for (long long i = b.base + threadIdx.x; i < end; i += blockDim.x) {
+        const uint32_t p = pid[i];
+        const bool ok = cell[i] >= 0 && (long long)p < R.n;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) out.a[k][i] = ok ? in.a[k][R.poff + p] : 0.f;
+    }
+}
+
+// One run's gradients in id order (doubles) and its load-parameter sums:
+// acc[0] = sum sign(pid) dJ/dvx (beam drift), acc[1] = sum dJ/dx . dx/dA.
+__global__ void ens_adj_export_kernel(const int32_t *__restrict__ cell, const uint32_t *__restrict__ pid,
+                                      CQuad4 a, long long from, long long to, long long n,
+                                      double *out, const double *dxdA, const double *dydA,
+                                      double *acc)
+{
+    __shared__ double s0[8], s1[8];
+    double b0 = 0.0, b1 = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = from + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < to; i += stride) {
+        const uint32_t p = pid[i];
+        if (cell[i] < 0 || (long long)p >= n) continue;
+        const double gx = a.a[0][i], gy = a.a[1][i], gvx = a.a[2][i], gvy = a.a[3][i];
+        if (out) {
+            out[p] = gx;
+            out[n + p] = gy;
+            out[2 * n + p] = gvx;
+            out[3 * n + p] = gvy;
+        }
+        b0 += (p & 1u) ? -gvx : gvx;
+        if (dxdA) b1 += gx * dxdA[p] + gy * dydA[p];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        b0 += __shfl_xor_sync(0xffffffffu, b0, o);
+        b1 += __shfl_xor_sync(0xffffffffu, b1, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s0[threadIdx.x >> 5] = b0;
+        s1[threadIdx.x >> 5] = b1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            t0 += s0[w];
+            t1 += s1[w];
+        }
+        atomicAdd(acc, t0);
+        atomicAdd(acc + 1, t1);
+    }
+}
+
+// ------------------------------------------------------------------ driver
+namespace {
+
+// device buffers of one adjoint run, freed on every exit path
+struct AdjBufs {
+    std::vector<void *> dev, host;
+    ~AdjBufs()
+    {
+        for (void *p : dev) cudaFree(p);
+        for (void *p : host) cudaFreeHost(p);
+    }
+    template <class T> pic_status dalloc(T **p, size_t n)
+    {
+        void *q = nullptr;
+        PIC_CUDA(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+        dev.push_back(q);
+        *p = (T *)q;
+        return PIC_OK;
+    }
+    // device memory if it is available, else pinned host memory (reached
+    // by the copies over the CPU-GPU link)
+    template <class T> pic_status any_alloc(T **p, size_t n, bool *on_host)
+    {
+        void *q = nullptr;
+        const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        if (cudaMalloc(&q, bytes) == cudaSuccess) {
+            dev.push_back(q);
+            *on_host = false;
+        } else {
+            cudaGetLastError();
+            PIC_CUDA(cudaMallocHost(&q, bytes));
+            host.push_back(q);
+            *on_host = true;
+        }
+        *p = (T *)q;
+        return PIC_OK;
+    }
+};
+
+struct Ckpt {
+    int32_t *cell;
+    float *ox, *oy, *vx, *vy;
+    uint32_t *pid;
+};
+
+pic_status ck_alloc(AdjBufs &B, Ckpt &C, size_t n, int *host_count)
+{
+    bool h[6];
+    PIC_TRY(B.any_alloc(&C.cell, n, &h[0]));
+    PIC_TRY(B.any_alloc(&C.ox, n, &h[1]));
+    PIC_TRY(B.any_alloc(&C.oy, n, &h[2]));
+    PIC_TRY(B.any_alloc(&C.vx, n, &h[3]));
+    PIC_TRY(B.any_alloc(&C.vy, n, &h[4]));
+    PIC_TRY(B.any_alloc(&C.pid, n, &h[5]));
+    for (bool x : h) *host_count += x ? 1 : 0;
+    return PIC_OK;
+}
+
+pic_status ck_copy(pic_ensemble *E, Ckpt &C, bool save)
+{
+    const size_t b = (size_t)E->nslots * 4;
+    void *live[6] = {E->cell[0], E->ox[0], E->oy[0], E->vx[0], E->vy[0], E->pid[0]};
+    void *ck[6] = {C.cell, C.ox, C.oy, C.vx, C.vy, C.pid};
+    for (int k = 0; k < 6; ++k)
+        PIC_CUDA(cudaMemcpyAsync(save ? ck[k] : live[k], save ? live[k] : ck[k], b,
+                                 cudaMemcpyDefault, E->stream));
+    return PIC_OK;
+}
+
+pic_status adj_plans(pic_ensemble *E)
+{
+    for (auto &G : E->groups) {
+        if (G.r2c2) continue;
+        const EnsRun &R = E->runs[G.first];
+        int dims[2] = {G.ny, G.nx}, real_emb[2] = {G.ny, G.nx}, cplx_emb[2] = {G.ny, R.nh};
+        // gx, gy of every run (stride ncp) -> gx^, gy^ (stride nk)
+        PIC_CUFFT(cufftPlanMany(&G.r2c2, 2, dims, real_emb, 1, (int)R.ncp, cplx_emb, 1, (int)R.nk,
+                                CUFFT_R2C, 2 * G.count));
+        PIC_CUFFT(cufftSetStream(G.r2c2, E->stream));
+        // psi^ (stride 2 nk) -> psi (stride ncp)
+        PIC_CUFFT(cufftPlanMany(&G.c2r1, 2, dims, cplx_emb, 1, (int)(2 * R.nk), real_emb, 1,
+                                (int)R.ncp, CUFFT_C2R, G.count));
+        PIC_CUFFT(cufftSetStream(G.c2r1, E->stream));
+    }
+    return PIC_OK;
+}
+
+}  // namespace
+
+pic_status ens_adjoint(pic_ensemble *E, const pic_init_spec *specs, long long nsteps, int every,
+                       double *gx0, double *gy0, double *gvx0, double *gvy0, pic_adjoint_result *out)
+{
+    if (nsteps < 1 || every < 1 || !specs) {
+        set_error("pic_ensemble_adjoint: needs specs, nsteps >= 1 and every >= 1");
+        return PIC_ERR_INVALID_ARG;
+    }
+    PIC_TRY(pic_ensemble_init(E, specs));
+    cudaStream_t st = E->stream;
+    const int nr = E->nruns;
+    const size_t ns = (size_t)E->nslots;
+    const int K = (int)std::min<long long>(every, nsteps);
+    const long long nseg = (nsteps + K - 1) / K;
+    AdjBufs B;
+    float *a[2][4], *g;
+    float2 *ghat;
+    for (int b = 0; b < 2; ++b)
+        for (int k = 0; k < 4; ++k) PIC_TRY(B.dalloc(&a[b][k], ns));
+    PIC_TRY(B.dalloc(&g, 2 * (size_t)E->nnodes));
+    PIC_TRY(B.dalloc(&ghat, (size_t)E->nmodes));
+    PIC_TRY(adj_plans(E));
+    std::vector<Ckpt> ck((size_t)nseg);  // ck[m-1]: state at step m K; ck[nseg-1]: final state
+    int on_host = 0;
+    for (auto &C : ck) PIC_TRY(ck_alloc(B, C, ns, &on_host));
+
+    // ---- forward with checkpoints
+    for (long long m = 1; m < nseg; ++m) {
+        PIC_TRY(pic_ensemble_step(E, K));
+        PIC_TRY(ck_copy(E, ck[(size_t)m - 1], true));
+    }
+    PIC_TRY(pic_ensemble_step(E, nsteps - (nseg - 1) * K));
+    PIC_TRY(ck_copy(E, ck[(size_t)nseg - 1], true));
+    PIC_TRY(pic_ensemble_synchronize(E));
+    // J per run, then the diagnostics state that the backward walk overwrites
+    std::vector<DevState> saved(nr);
+    PIC_CUDA(cudaMemcpy(saved.data(), E->dev, sizeof(DevState) * nr, cudaMemcpyDeviceToHost));
+    const size_t hist_n = (size_t)nr * 6 * E->hist_cap;
+    std::vector<double> hist_saved(hist_n);
+    PIC_CUDA(cudaMemcpy(hist_saved.data(), E->hist, hist_n * 8, cudaMemcpyDeviceToHost));
+    const int since_saved = E->since_sort;
+
+    EnsAdjArgs A;
+    A.e = E->e;
+    A.g = g;
+    A.psi = E->rho;
+    int cur = 0;
+    auto set_arrays = [&]() {
+        A.cell = E->cell[0];
+        A.ox = E->ox[0];
+        A.oy = E->oy[0];
+        A.vx = E->vx[0];
+        A.vy = E->vy[0];
+        A.ax = a[cur][0];
+        A.ay = a[cur][1];
+        A.avx = a[cur][2];
+        A.avy = a[cur][3];
+    };
+    auto solve_gather = [&]() -> pic_status {
+        for (auto &G : E->groups) {
+            const EnsRun &R = E->runs[G.first];
+            PIC_CUFFT(cufftExecR2C(G.r2c2, g + 2 * R.goff, (cufftComplex *)(ghat + R.khoff)));
+        }
+        ens_adj_kspace_kernel<<<E->nmode_blk, 256, 0, st>>>(ghat, E->rhohat, E->mode_blk, E->d_runs);
+        PIC_CUDA(cudaGetLastError());
+        for (auto &G : E->groups) {
+            const EnsRun &R = E->runs[G.first];
+            PIC_CUFFT(cufftExecC2R(G.c2r1, (cufftComplex *)(E->rhohat + R.khoff), E->rho + R.goff));
+        }
+        set_arrays();
+        ens_adj_gather_kernel<<<E->npush, 256, 0, st>>>(A, E->push_blk, E->d_runs);
+        PIC_CUDA(cudaGetLastError());
+        return PIC_OK;
+    };
+    auto kick = [&](bool unkick, float cscale, float dscale) -> pic_status {
+        PIC_CUDA(cudaMemsetAsync(g, 0, sizeof(float) * 2 * (size_t)E->nnodes, st));
+        set_arrays();
+        if (unkick)
+            ens_adj_kick_kernel<true><<<E->npush, 256, E->push_smem, st>>>(A, E->push_blk, E->d_runs,
+                                                                       E->anchor, cscale, dscale);
+        else
+            ens_adj_kick_kernel<false><<<E->npush, 256, E->push_smem, st>>>(A, E->push_blk, E->d_runs,
+                                                                        E->anchor, cscale, dscale);
+        PIC_CUDA(cudaGetLastError());
+        return solve_gather();
+    };
+    auto quad = [&](int b) {
+        Quad4 q;
+        for (int k = 0; k < 4; ++k) q.a[k] = a[b][k];
+        return q;
+    };
+    auto cquad = [&](int b) {
+        CQuad4 q;
+        for (int k = 0; k < 4; ++k) q.a[k] = a[b][k];
+        return q;
+    };
+
+    // ---- terminal condition a_x = grad J(x_N), a_v = 0
+    for (int k = 0; k < 4; ++k) PIC_CUDA(cudaMemsetAsync(a[cur][k], 0, ns * 4, st));
+    ens_adj_terminal_kernel<<<E->nnode_blk, 256, 0, st>>>(E->e, g, E->node_blk, E->d_runs);
+    PIC_CUDA(cudaGetLastError());
+    PIC_TRY(solve_gather());
+
+    // ---- backward walk
+    const int S = E->sort_every;
+    int since = 0;
+    for (long long s = nsteps - 1; s >= 0; --s) {
+        if ((s + 1) % K == 0 && s + 1 < nsteps) {
+            // exact state at s + 1: adjoint arrays into the checkpoint's order
+            ens_to_id_kernel<<<E->nsort, 256, 0, st>>>(E->cell[0], E->pid[0], cquad(cur), quad(1 - cur),
+                                                       E->sort_blk, E->d_runs);
+            PIC_CUDA(cudaGetLastError());
+            PIC_TRY(ck_copy(E, ck[(size_t)((s + 1) / K - 1)], false));
+            ens_from_id_kernel<<<E->nsort, 256, 0, st>>>(E->cell[0], E->pid[0], cquad(1 - cur), quad(cur),
+                                                         E->sort_blk, E->d_runs);
+            PIC_CUDA(cudaGetLastError());
+            since = S;
+        }
+        int src = 0;
+        if (since >= S) {
+            const float *xin[4] = {a[cur][0], a[cur][1], a[cur][2], a[cur][3]};
+            float *xout[4] = {a[1 - cur][0], a[1 - cur][1], a[1 - cur][2], a[1 - cur][3]};
+            PIC_TRY(ens_sort(E, xin, xout));
+            cur ^= 1;
+            src = 1;
+            since = 0;
+        }
+        PIC_TRY(ens_launch_push(E, src, 3));  // x_s, deposit
+        PIC_TRY(ens_poisson(E));              // E(x_s)
+        PIC_TRY(kick(true, 1.f, 1.f));
+        ++since;
+    }
+    PIC_TRY(kick(false, -0.5f, 0.f));  // the priming half kick
+
+    // ---- outputs
+    std::vector<double> acc(2 * (size_t)nr, 0.0);
+    double *d_acc, *stage = nullptr, *dA = nullptr;
+    PIC_TRY(B.dalloc(&d_acc, 2 * (size_t)nr));
+    PIC_CUDA(cudaMemsetAsync(d_acc, 0, 16 * (size_t)nr, st));
+    long long nmax = 0;
+    for (const EnsRun &R : E->runs) nmax = std::max(nmax, R.n);
+    const bool want = gx0 || gy0 || gvx0 || gvy0;
+    if (want) PIC_TRY(B.dalloc(&stage, 4 * (size_t)nmax));
+    PIC_TRY(B.dalloc(&dA, 2 * (size_t)nmax));
+    std::vector<long long> first(nr, 0);
+    for (int r = 1; r < nr; ++r) first[r] = first[r - 1] + specs[r - 1].n;
+    std::vector<double> host;
+    for (int r = 0; r < nr; ++r) {
+        const int sidx = E->slot_of[r];
+        const EnsRun &R = E->runs[sidx];
+        const pic_init_spec &sp = specs[r];
+        const bool amp_kind = sp.pert_kind == PIC_PERT_XDISP || sp.pert_kind == PIC_PERT_DENSITY;
+        if (amp_kind && R.n) {
+            int lx = 0, ly = 0;
+            if (sp.layout == PIC_LOAD_LATTICE)
+                PIC_TRY(lattice_dims_for(R.nx, R.ny, R.n, &lx, &ly));
+            InitTarget T;
+            memset(&T, 0, sizeof T);
+            T.nx = R.nx;
+            T.ny = R.ny;
+            T.Lx = E->cfg[r].Lx;
+            T.Ly = E->cfg[r].Ly;
+            PIC_TRY(launch_init_dA_target(T, &sp, lx, ly, dA, dA + R.n, st));
+        }
+        ens_adj_export_kernel<<<grid_for(R.cap4, 256), 256, 0, st>>>(
+            E->cell[0], E->pid[0], cquad(cur), R.poff, R.poff + R.cap4, R.n, want ? stage : nullptr,
+            amp_kind ? dA : nullptr, amp_kind ? dA + R.n : nullptr, d_acc + 2 * r);
+        PIC_CUDA(cudaGetLastError());
+        if (want && R.n) {
+            host.resize(4 * (size_t)R.n);
+            PIC_CUDA(cudaMemcpyAsync(host.data(), stage, host.size() * 8, cudaMemcpyDeviceToHost, st));
+            PIC_CUDA(cudaStreamSynchronize(st));
+            double *dst[4] = {gx0, gy0, gvx0, gvy0};
+            for (int k = 0; k < 4; ++k)
+                if (dst[k]) std::copy(host.begin() + k * R.n, host.begin() + (k + 1) * R.n, dst[k] + first[r]);
+        }
+    }
+    PIC_CUDA(cudaMemcpyAsync(acc.data(), d_acc, 16 * (size_t)nr, cudaMemcpyDeviceToHost, st));
+    // ---- leave the ensemble at step nsteps
+    PIC_TRY(ck_copy(E, ck[(size_t)nseg - 1], false));
+    PIC_TRY(ens_launch_push(E, 0, 2));  // deposit in place
+    PIC_TRY(ens_poisson(E));
+    PIC_CUDA(cudaMemcpyAsync(E->dev, saved.data(), sizeof(DevState) * nr, cudaMemcpyHostToDevice, st));
+    PIC_CUDA(cudaMemcpyAsync(E->hist, hist_saved.data(), hist_n * 8, cudaMemcpyHostToDevice, st));
+    PIC_CUDA(cudaStreamSynchronize(st));
+    E->since_sort = std::max(since_saved, S);  // anchors are stale: sort before the next step
+    if (out) {
+        for (int r = 0; r < nr; ++r) {
+            const int sidx = E->slot_of[r];
+            const long long step = saved[sidx].step;
+            out[r].J = hist_saved[(size_t)sidx * 6 * E->hist_cap + (size_t)(step % E->hist_cap)];
+            out[r].dJ_dbeam_v = acc[2 * r];
+            out[r].dJ_damp = acc[2 * r + 1];
+        }
+    }
+    (void)on_host;
+    return PIC_OK;
+}
+
+}  // namespace pic
+
+extern "C" pic_status pic_ensemble_adjoint(pic_ensemble *e, const pic_init_spec *specs,
+                                           long long nsteps, int every, double *dJ_dx0,
+                                           double *dJ_dy0, double *dJ_dvx0, double *dJ_dvy0,
+                                           pic_adjoint_result *out)
+{
+    PIC_TRY(pic::ens_need(e, -1));
+    return pic::ens_adjoint(e, specs, nsteps, every, dJ_dx0, dJ_dy0, dJ_dvx0, dJ_dvy0, out);
+}

@@ -23,6 +23,8 @@
 // and every push chunk knows the tile of its first particle (anchor).
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "pic_sort_dev.cuh"
 
 namespace pic {
@@ -202,6 +204,7 @@ pic_status launch_sort(pic_handle *h, int s)
     if (B.cap == 0) return PIC_OK;
     const long long ncell = (long long)g.nx * g.ny;
     SortArgs A;
+    memset(&A, 0, sizeof A);
     A.cin = B.cell[0];
     A.oxin = B.ox[0];
     A.oyin = B.oy[0];

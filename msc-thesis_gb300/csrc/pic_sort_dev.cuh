@@ -31,6 +31,8 @@ struct SortArgs {
     int nx, ny, tw, th, ntx, chunk;
     long long nkeys;  // keys of the whole key space (cells + empty bins)
     unsigned int *err;
+    const uint32_t *xin[4];  // optional extra per-particle arrays moved along
+    uint32_t *xout[4];       // (all four or none)
 };
 
 // Key geometry of the run a sort block works on: the run's grid and tiles
@@ -330,6 +332,14 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
         const uint32_t *const src[3] = {reinterpret_cast<const uint32_t *>(A.vzin), nullptr, nullptr};
         uint32_t *const dst[3] = {reinterpret_cast<uint32_t *>(A.vzout), nullptr, nullptr};
         stage_fields<1>(S, base, end, keys, src, dst);
+    }
+    if (A.xin[0]) {
+        const uint32_t *const src[3] = {A.xin[0], A.xin[1], A.xin[2]};
+        uint32_t *const dst[3] = {A.xout[0], A.xout[1], A.xout[2]};
+        stage_fields<3>(S, base, end, keys, src, dst);
+        const uint32_t *const src1[3] = {A.xin[3], nullptr, nullptr};
+        uint32_t *const dst1[3] = {A.xout[3], nullptr, nullptr};
+        stage_fields<1>(S, base, end, keys, src1, dst1);
     }
 }
 

@@ -156,6 +156,7 @@ SIGNATURES = {
     "pic_ensemble_get_history": [_H, C.c_int, C.c_int, C.c_longlong, C.c_longlong, _vp],
     "pic_ensemble_get_particles": [_H, C.c_int, C.POINTER(C.c_longlong), _vp, _vp, _vp, _vp],
     "pic_ensemble_autotune": [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p],
+    "pic_ensemble_adjoint": [_H, C.c_void_p, C.c_longlong, C.c_int, _vp, _vp, _vp, _vp, C.c_void_p],
     "pic_run_host": [_H, C.c_longlong, _vp, _vp, _vp, _vp, C.c_longlong, C.c_int,
                      _vp, _vp, _vp, _vp],
     "pic_diagnostics": [_H, C.POINTER(Diag)],
@@ -559,6 +560,24 @@ class Ensemble:
         out = np.empty(count)
         self._c("pic_ensemble_get_history", run, which, first, count, _ptr(out))
         return out
+
+    def adjoint(self, specs, nsteps, every=50, gradients=True):
+        """pic_ensemble_adjoint: per run (J, dJ/d beam_v, dJ/d pert_amp) and, with
+        gradients, per run the arrays (dJ/dx0, dJ/dy0, dJ/dvx0, dJ/dvy0) in id order."""
+        sp = (InitSpec * len(specs))(*specs)
+        res = (AdjointResult * len(specs))()
+        total = sum(int(x.n) for x in specs)
+        arrs = [np.empty(total) for _ in range(4)] if gradients else [None] * 4
+        self._c("pic_ensemble_adjoint", C.addressof(sp), int(nsteps), int(every),
+                *[_ptr(a) for a in arrs], C.addressof(res))
+        out = [(r.J, r.dJ_dbeam_v, r.dJ_damp) for r in res]
+        if not gradients:
+            return out, None
+        per, k = [], 0
+        for x in specs:
+            per.append(tuple(a[k:k + x.n] for a in arrs))
+            k += x.n
+        return out, per
 
     def get_particles(self, run):
         n = C.c_longlong()

@@ -1,0 +1,117 @@
+"""Ensemble adjoint (pic_ensemble_adjoint) against the single-run GPU adjoint,
+the FP64 adjoint restatement and central finite differences."""
+import numpy as np
+import pytest
+
+import oracle as O
+import picgpu as P
+from gpu_util import normalized_electrons
+
+pytestmark = pytest.mark.gpu
+
+L = 4 * np.pi
+DT = 0.1
+# (nx, ny, particles per cell, beam drift, x-displacement amplitude, seed)
+RUNS = [(32, 32, 16, 0.2, 1e-3, 11), (64, 32, 8, 0.15, 3e-3, 12), (32, 32, 32, 0.25, 1e-2, 13)]
+
+
+def setup(runs, **tuning):
+    cfgs, specs, qm = [], [], []
+    for nx, ny, ppc, v0, amp, seed in runs:
+        n = nx * ny * ppc
+        cfg, q, m = normalized_electrons(nx, ny, L, L, n, DT, **tuning)
+        cfgs.append(cfg)
+        specs.append(P.init_spec(n, vth=(0.01, 0.01, 0.0), beam_v=v0, pert_kind=P.PERT_XDISP,
+                                 pert_amp=amp, pert_mx=1, seed=seed))
+        qm.append((q, m))
+    return cfgs, specs, qm
+
+
+def rel_norm(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_ensemble_adjoint_matches_single_run_and_fp64():
+    nst, every = 40, 15
+    cfgs, specs, qm = setup(RUNS, sort_every=5)
+    with P.Ensemble(cfgs) as E:
+        res, grads = E.adjoint(specs, nst, every)
+        E.synchronize()
+        assert all(E.diagnostics(r).step == nst for r in range(len(RUNS)))
+    for r, (cfg, spec) in enumerate(zip(cfgs, specs)):
+        with P.Handle(cfg) as h:
+            h.init_particles(0, spec)
+            s0 = h.get_particles(0)
+            single, *sg = h.adjoint(nst, every=8, spec=spec)
+        q, m = qm[r]
+        ocfg = O.PhysCfg(cfg.nx, cfg.ny, L, L, DT, 1.0, 1)
+        J, *og = O.adjoint(ocfg, s0["x"], s0["y"], s0["vx"], s0["vy"], q, m, nst)
+        errs_single = [rel_norm(a, b) for a, b in zip(grads[r], sg)]
+        errs_fp64 = [rel_norm(a, b) for a, b in zip(grads[r], og)]
+        print(f"run {r}: J {res[r][0]:.6e} single {single.J:.6e} fp64 {J:.6e}; "
+              f"vs single {max(errs_single):.2e}, vs FP64 {max(errs_fp64):.2e}; "
+              f"dbeam {res[r][1]:.6e} / {single.dJ_dbeam_v:.6e}, damp {res[r][2]:.6e} / {single.dJ_damp:.6e}")
+        assert res[r][0] == pytest.approx(single.J, rel=1e-5)
+        assert res[r][0] == pytest.approx(J, rel=1e-4)
+        assert max(errs_single) < 2e-3
+        assert max(errs_fp64) < 2e-3
+        assert res[r][1] == pytest.approx(single.dJ_dbeam_v, rel=2e-3)
+        assert res[r][2] == pytest.approx(single.dJ_damp, rel=2e-3)
+
+
+def test_ensemble_adjoint_against_central_differences():
+    """dJ/d(beam drift) and dJ/d(amplitude) against central differences
+    (eps 1e-4) of the FP64 oracle's forward map from the same loads.  The
+    differences cross cell boundaries (CIC kinks), so the bar is 1e-2."""
+    nst = 30
+    runs = RUNS[:2]
+    cfgs, specs, qm = setup(runs)
+    with P.Ensemble(cfgs) as E:
+        res, _ = E.adjoint(specs, nst, every=10, gradients=False)
+    for r, (nx, ny, ppc, v0, amp, seed) in enumerate(runs):
+        cfg = cfgs[r]
+        q, m = qm[r]
+        ocfg = O.PhysCfg(nx, ny, L, L, DT, 1.0, 1)
+        eps = 1e-4
+        fd = {}
+        for key in ("beam", "amp"):
+            vals = []
+            for e in (eps, -eps):
+                sp = P.init_spec(nx * ny * ppc, vth=(0.01, 0.01, 0.0),
+                                 beam_v=v0 + (e if key == "beam" else 0.0), pert_kind=P.PERT_XDISP,
+                                 pert_amp=amp + (e if key == "amp" else 0.0), pert_mx=1, seed=seed)
+                with P.Handle(cfg) as h:
+                    h.init_particles(0, sp)
+                    s0 = h.get_particles(0)
+                vals.append(O.forward_J(ocfg, s0["x"], s0["y"], s0["vx"], s0["vy"], q, m, nst))
+            fd[key] = (vals[0] - vals[1]) / (2 * eps)
+        print(f"run {r}: dJ/dbeam adjoint {res[r][1]:.6e} FD {fd['beam']:.6e}; "
+              f"dJ/damp adjoint {res[r][2]:.6e} FD {fd['amp']:.6e}")
+        assert res[r][1] == pytest.approx(fd["beam"], rel=1e-2)
+        assert res[r][2] == pytest.approx(fd["amp"], rel=1e-2)
+
+
+def test_ensemble_adjoint_checkpoint_spacing_and_final_state():
+    nst = 36
+    cfgs, specs, _ = setup(RUNS, sort_every=4)
+    out = {}
+    for every in (6, 36):
+        with P.Ensemble(cfgs) as E:
+            out[every] = E.adjoint(specs, nst, every)
+            final = [E.get_particles(r) for r in range(len(RUNS))]
+            E.step(3)
+            after = [E.get_particles(r) for r in range(len(RUNS))]
+        with P.Ensemble(cfgs) as F:
+            F.init(specs)
+            F.step(nst)
+            ref = [F.get_particles(r) for r in range(len(RUNS))]
+            F.step(3)
+            ref_after = [F.get_particles(r) for r in range(len(RUNS))]
+        for r in range(len(RUNS)):
+            for k in ref[r]:
+                np.testing.assert_array_equal(final[r][k], ref[r][k])
+                np.testing.assert_array_equal(after[r][k], ref_after[r][k])
+    for r in range(len(RUNS)):
+        assert out[6][0][r][0] == out[36][0][r][0]
+        for a, b in zip(out[6][1][r], out[36][1][r]):
+            assert rel_norm(a, b) < 2e-3
