@@ -236,7 +236,7 @@ def bench_ensemble(args):
     if rank != 0:
         return
     torch.cuda.set_device(local)
-    cfgs, specs, grids, ppcs = c5_runs(P, local=local)
+    cfgs, specs, grids, ppcs = c5_runs(P, nruns=args.runs, local=local)
     total = sum(int(s.n) for s in specs)
     tune = None
     if args.no_tune:
@@ -311,7 +311,7 @@ def bench_ensemble(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "ensemble-64-two-stream", "runs": len(cfgs), "particles": total,
+        "config": {"workload": f"ensemble-{len(cfgs)}-two-stream", "runs": len(cfgs), "particles": total,
                    "cells": cells, "grid_counts": {str(k): int((grids == k).sum()) for k in (64, 128, 256, 512)},
                    "chunk": int(cfgs[0].chunk), "sort_every": S, "sorts_in_timed_steps": ens_sorts,
                    "tune_ms_per_step": tune.ms_per_step if tune else None,
@@ -346,6 +346,7 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=500,
                     help="ensemble workload: steps of the timed forward+adjoint (0: skip)")
     ap.add_argument("--every", type=int, default=50, help="adjoint checkpoint spacing")
+    ap.add_argument("--runs", type=int, default=64, help="ensemble workload: runs (profiling on fewer)")
     ap.add_argument("--no-plain", action="store_true",
                     help="ensemble workload: skip the one-run-at-a-time comparison")
     ap.add_argument("--workload", default="landau", choices=["landau", "ensemble"],

@@ -65,12 +65,54 @@ __device__ __forceinline__ PushGeo adj_geo(const EnsRun &R, const float *e)
     return G;
 }
 
+// Sums v[0..7] over each maximal run of consecutive lanes with the same key
+// (particles are cell-sorted, so a warp holds few runs); true on the run's
+// first lane, which then holds the run's totals.  Every lane of the warp
+// must call it; key -1 marks a lane without a particle.  Lane i adds the
+// partial of lane i + o only while i + o is before the next run start.
+__device__ __forceinline__ bool warp_run_sum8(int key, float (&v)[8])
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(full, key, 1);
+    const bool head = lane == 0 || key != prev;
+    const unsigned heads = __ballot_sync(full, head);
+    const unsigned after = heads & (0xfffffffeu << lane);
+    const int seg_end = after ? __ffs(after) - 1 : 32;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float t = __shfl_down_sync(full, v[k], o);
+            if (lane + o < seg_end) v[k] += t;
+        }
+    }
+    return head;
+}
+
+__device__ __forceinline__ void red_cell(float *gx, float *gy, int c, int nx, int ny, const float (&v)[8])
+{
+    const Cic w = cic_of(c, 0.f, 0.f, nx, ny);
+    atomicAdd(gx + w.i00, v[0]);
+    atomicAdd(gy + w.i00, v[1]);
+    atomicAdd(gx + w.i10, v[2]);
+    atomicAdd(gy + w.i10, v[3]);
+    atomicAdd(gx + w.i01, v[4]);
+    atomicAdd(gy + w.i01, v[5]);
+    atomicAdd(gx + w.i11, v[6]);
+    atomicAdd(gy + w.i11, v[7]);
+}
+
 // Drift adjoint, kick transpose (scatter of mu and local term) and, with
 // UNKICK, the reversal of the kick.  One push block of particles per CTA;
-// E and the scatter accumulators of the block's window live in shared
-// memory (the push window layout, accumulators as floats).
+// each lane owns four consecutive particles (128-bit loads), E comes from
+// the block's shared-memory window (global loads outside it).  Scatter
+// contributions are summed in registers over a lane's particles in one
+// cell, then over the warp's lanes in one cell (warp_run_sum8), and added
+// to the global planes by the run's first lane (shared-memory float
+// atomics measured slower than these global reductions).
 template <bool UNKICK>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs,
                     const int32_t *__restrict__ anchor, float cscale, float dscale)
 {
@@ -79,85 +121,106 @@ ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun
     const EnsRun &R = runs[b.run];
     const PushGeo G = adj_geo(R, A.e);
     const Window W = setup_window(G, smem, anchor[blockIdx.x]);
-    load_window<true, true>(G, W);  // E into sE, accumulators zeroed
+    load_window<true, false>(G, W);
     __syncthreads();
-    float *sgx = reinterpret_cast<float *>(W.sLo), *sgy = reinterpret_cast<float *>(W.sHi);
     float *ggx = A.g + 2 * R.goff, *ggy = ggx + R.ncp;
     const float qmdt = R.qm_dt, muc = cscale * R.qm_dt, ddt = dscale * R.dt;
     const int nx = R.nx, ny = R.ny;
-    const long long end = b.base + b.count;
-    for (long long i = b.base + threadIdx.x; i < end; i += blockDim.x) {
-        const int c = A.cell[i];
-        const int cx = c & 0xFFFF, cy = c >> 16;
-        if (c < 0 || cx >= nx || cy >= ny) continue;
-        const float ox = A.ox[i], oy = A.oy[i];
-        const float ax = A.ax[i], ay = A.ay[i];
-        const float avx = fmaf(ddt, ax, A.avx[i]), avy = fmaf(ddt, ay, A.avy[i]);
-        const float mx = muc * avx, my = muc * avy;
-        const float gx = 1.f - ox, gy = 1.f - oy;
-        const float w00 = gx * gy, w10 = ox * gy, w01 = gx * oy, w11 = ox * oy;
-        float2 e00, e10, e01, e11;
-        int dxl = cx - W.wx0, dyl = cy - W.wy0;
-        if (dxl < 0) dxl += nx;
-        if (dyl < 0) dyl += ny;
-        if (W.on && dxl < G.wcx && dyl < G.wcy) {
-            const int l = dyl * W.nwx + dxl;
-            e00 = W.sE[l];
-            e10 = W.sE[l + 1];
-            e01 = W.sE[l + W.nwx];
-            e11 = W.sE[l + W.nwx + 1];
-            atomicAdd(sgx + l, w00 * mx);
-            atomicAdd(sgy + l, w00 * my);
-            atomicAdd(sgx + l + 1, w10 * mx);
-            atomicAdd(sgy + l + 1, w10 * my);
-            atomicAdd(sgx + l + W.nwx, w01 * mx);
-            atomicAdd(sgy + l + W.nwx, w01 * my);
-            atomicAdd(sgx + l + W.nwx + 1, w11 * mx);
-            atomicAdd(sgy + l + W.nwx + 1, w11 * my);
-        } else {
-            const Cic w = cic_of(c, ox, oy, nx, ny);
-            e00 = make_float2(G.ex[w.i00], G.ey[w.i00]);
-            e10 = make_float2(G.ex[w.i10], G.ey[w.i10]);
-            e01 = make_float2(G.ex[w.i01], G.ey[w.i01]);
-            e11 = make_float2(G.ex[w.i11], G.ey[w.i11]);
-            atomicAdd(ggx + w.i00, w00 * mx);
-            atomicAdd(ggy + w.i00, w00 * my);
-            atomicAdd(ggx + w.i10, w10 * mx);
-            atomicAdd(ggy + w.i10, w10 * my);
-            atomicAdd(ggx + w.i01, w01 * mx);
-            atomicAdd(ggy + w.i01, w01 * my);
-            atomicAdd(ggx + w.i11, w11 * mx);
-            atomicAdd(ggy + w.i11, w11 * my);
+    const long long end = b.base + b.count;  // a multiple of 4 from base
+    const long long lane4 = 4ll * (threadIdx.x & 31);
+    for (long long qw = b.base + 4ll * (threadIdx.x & ~31u); qw < end; qw += 4ll * blockDim.x) {
+        const long long q = qw + lane4;
+        const bool live = q < end;
+        int cc[4] = {-1, -1, -1, -1};
+        float ox[4], oy[4], ax[4], ay[4], avx[4], avy[4], vx[4], vy[4];
+        if (live) {
+            const int4 c4 = *reinterpret_cast<const int4 *>(A.cell + q);
+            const float4 a4 = *reinterpret_cast<const float4 *>(A.ox + q);
+            const float4 b4 = *reinterpret_cast<const float4 *>(A.oy + q);
+            const float4 x4 = *reinterpret_cast<const float4 *>(A.ax + q);
+            const float4 y4 = *reinterpret_cast<const float4 *>(A.ay + q);
+            const float4 u4 = *reinterpret_cast<const float4 *>(A.avx + q);
+            const float4 w4 = *reinterpret_cast<const float4 *>(A.avy + q);
+            cc[0] = c4.x, cc[1] = c4.y, cc[2] = c4.z, cc[3] = c4.w;
+            ox[0] = a4.x, ox[1] = a4.y, ox[2] = a4.z, ox[3] = a4.w;
+            oy[0] = b4.x, oy[1] = b4.y, oy[2] = b4.z, oy[3] = b4.w;
+            ax[0] = x4.x, ax[1] = x4.y, ax[2] = x4.z, ax[3] = x4.w;
+            ay[0] = y4.x, ay[1] = y4.y, ay[2] = y4.z, ay[3] = y4.w;
+            avx[0] = u4.x, avx[1] = u4.y, avx[2] = u4.z, avx[3] = u4.w;
+            avy[0] = w4.x, avy[1] = w4.y, avy[2] = w4.z, avy[3] = w4.w;
+            if (UNKICK) {
+                const float4 p4 = *reinterpret_cast<const float4 *>(A.vx + q);
+                const float4 r4 = *reinterpret_cast<const float4 *>(A.vy + q);
+                vx[0] = p4.x, vx[1] = p4.y, vx[2] = p4.z, vx[3] = p4.w;
+                vy[0] = r4.x, vy[1] = r4.y, vy[2] = r4.z, vy[3] = r4.w;
+            }
         }
-        const float s00 = e00.x * mx + e00.y * my, s10 = e10.x * mx + e10.y * my;
-        const float s01 = e01.x * mx + e01.y * my, s11 = e11.x * mx + e11.y * my;
-        A.ax[i] = ax + (gy * (s10 - s00) + oy * (s11 - s01)) * R.inv_dx;
-        A.ay[i] = ay + (gx * (s01 - s00) + ox * (s11 - s10)) * R.inv_dy;
-        A.avx[i] = avx;
-        A.avy[i] = avy;
-        if (UNKICK) {  // the push's gather, then the kick taken back
-            const float Ex = gy * fmaf(gx, e00.x, ox * e10.x) + oy * fmaf(gx, e01.x, ox * e11.x);
-            const float Ey = gy * fmaf(gx, e00.y, ox * e10.y) + oy * fmaf(gx, e01.y, ox * e11.y);
-            A.vx[i] = fmaf(-qmdt, Ex, A.vx[i]);
-            A.vy[i] = fmaf(-qmdt, Ey, A.vy[i]);
+        int gkey = -1;
+        float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = cc[j];
+            const int cx = c & 0xFFFF, cy = c >> 16;
+            if (c < 0 || cx >= nx || cy >= ny) continue;
+            const float avxj = fmaf(ddt, ax[j], avx[j]), avyj = fmaf(ddt, ay[j], avy[j]);
+            const float mx = muc * avxj, my = muc * avyj;
+            const float gx = 1.f - ox[j], gy = 1.f - oy[j];
+            const float w00 = gx * gy, w10 = ox[j] * gy, w01 = gx * oy[j], w11 = ox[j] * oy[j];
+            float2 e00, e10, e01, e11;
+            int dxl = cx - W.wx0, dyl = cy - W.wy0;
+            if (dxl < 0) dxl += nx;
+            if (dyl < 0) dyl += ny;
+            if (W.on && dxl < G.wcx && dyl < G.wcy) {
+                const int l = dyl * W.nwx + dxl;
+                e00 = W.sE[l];
+                e10 = W.sE[l + 1];
+                e01 = W.sE[l + W.nwx];
+                e11 = W.sE[l + W.nwx + 1];
+            } else {
+                const Cic w = cic_of(c, 0.f, 0.f, nx, ny);
+                e00 = make_float2(G.ex[w.i00], G.ey[w.i00]);
+                e10 = make_float2(G.ex[w.i10], G.ey[w.i10]);
+                e01 = make_float2(G.ex[w.i01], G.ey[w.i01]);
+                e11 = make_float2(G.ex[w.i11], G.ey[w.i11]);
+            }
+            const float v[8] = {w00 * mx, w00 * my, w10 * mx, w10 * my,
+                                w01 * mx, w01 * my, w11 * mx, w11 * my};
+            if (gkey < 0) gkey = c;
+            if (c == gkey) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) acc[k] += v[k];
+            } else {
+                red_cell(ggx, ggy, c, nx, ny, v);
+            }
+            const float s00 = e00.x * mx + e00.y * my, s10 = e10.x * mx + e10.y * my;
+            const float s01 = e01.x * mx + e01.y * my, s11 = e11.x * mx + e11.y * my;
+            ax[j] += (gy * (s10 - s00) + oy[j] * (s11 - s01)) * R.inv_dx;
+            ay[j] += (gx * (s01 - s00) + ox[j] * (s11 - s10)) * R.inv_dy;
+            avx[j] = avxj;
+            avy[j] = avyj;
+            if (UNKICK) {  // the push's gather, then the kick taken back
+                const float Ex = gy * fmaf(gx, e00.x, ox[j] * e10.x) + oy[j] * fmaf(gx, e01.x, ox[j] * e11.x);
+                const float Ey = gy * fmaf(gx, e00.y, ox[j] * e10.y) + oy[j] * fmaf(gx, e01.y, ox[j] * e11.y);
+                vx[j] = fmaf(-qmdt, Ex, vx[j]);
+                vy[j] = fmaf(-qmdt, Ey, vy[j]);
+            }
         }
-    }
-    __syncthreads();
-    if (W.on) {
-        for (int k = threadIdx.x; k < W.nw; k += blockDim.x) {
-            const float vx = sgx[k], vy = sgy[k];
-            if (vx != 0.f || vy != 0.f) {
-                const int a = k % W.nwx, bb = k / W.nwx;
-                const int gxn = (W.wx0 + a) % nx, gyn = (W.wy0 + bb) % ny;
-                const long long node = (long long)gyn * nx + gxn;
-                atomicAdd(ggx + node, vx);
-                atomicAdd(ggy + node, vy);
+        if (warp_run_sum8(gkey, acc) && gkey >= 0) red_cell(ggx, ggy, gkey, nx, ny, acc);
+        if (live) {
+            *reinterpret_cast<float4 *>(A.ax + q) = make_float4(ax[0], ax[1], ax[2], ax[3]);
+            *reinterpret_cast<float4 *>(A.ay + q) = make_float4(ay[0], ay[1], ay[2], ay[3]);
+            *reinterpret_cast<float4 *>(A.avx + q) = make_float4(avx[0], avx[1], avx[2], avx[3]);
+            *reinterpret_cast<float4 *>(A.avy + q) = make_float4(avy[0], avy[1], avy[2], avy[3]);
+            if (UNKICK) {
+                *reinterpret_cast<float4 *>(A.vx + q) = make_float4(vx[0], vx[1], vx[2], vx[3]);
+                *reinterpret_cast<float4 *>(A.vy + q) = make_float4(vy[0], vy[1], vy[2], vy[3]);
             }
         }
     }
 }
 
-// adjoint of the deposit: a_x += (q/dA) sum_m psi_m grad w_m
+// adjoint of the deposit: a_x += (q/dA) sum_m psi_m grad w_m (four
+// consecutive particles per thread, 128-bit loads)
 __global__ void __launch_bounds__(256)
 ens_adj_gather_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
 {
@@ -165,13 +228,26 @@ ens_adj_gather_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsR
     const EnsRun &R = runs[b.run];
     const float *psi = A.psi + R.goff;
     const long long end = b.base + b.count;
-    for (long long i = b.base + threadIdx.x; i < end; i += blockDim.x) {
-        const Cic w = cic_of(A.cell[i], A.ox[i], A.oy[i], R.nx, R.ny);
-        if (!w.ok) continue;
-        const float2 g = grad_dot(w, psi[w.i00], psi[w.i10], psi[w.i01], psi[w.i11], R.inv_dx,
-                                  R.inv_dy);
-        A.ax[i] = fmaf(R.q_dA, g.x, A.ax[i]);
-        A.ay[i] = fmaf(R.q_dA, g.y, A.ay[i]);
+    for (long long q = b.base + 4ll * threadIdx.x; q < end; q += 4ll * blockDim.x) {
+        const int4 c4 = *reinterpret_cast<const int4 *>(A.cell + q);
+        const float4 a4 = *reinterpret_cast<const float4 *>(A.ox + q);
+        const float4 b4 = *reinterpret_cast<const float4 *>(A.oy + q);
+        float4 x4 = *reinterpret_cast<const float4 *>(A.ax + q);
+        float4 y4 = *reinterpret_cast<const float4 *>(A.ay + q);
+        const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+        const float ox[4] = {a4.x, a4.y, a4.z, a4.w}, oy[4] = {b4.x, b4.y, b4.z, b4.w};
+        float ax[4] = {x4.x, x4.y, x4.z, x4.w}, ay[4] = {y4.x, y4.y, y4.z, y4.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const Cic w = cic_of(cc[j], ox[j], oy[j], R.nx, R.ny);
+            if (!w.ok) continue;
+            const float2 g = grad_dot(w, psi[w.i00], psi[w.i10], psi[w.i01], psi[w.i11], R.inv_dx,
+                                      R.inv_dy);
+            ax[j] = fmaf(R.q_dA, g.x, ax[j]);
+            ay[j] = fmaf(R.q_dA, g.y, ay[j]);
+        }
+        *reinterpret_cast<float4 *>(A.ax + q) = make_float4(ax[0], ax[1], ax[2], ax[3]);
+        *reinterpret_cast<float4 *>(A.ay + q) = make_float4(ay[0], ay[1], ay[2], ay[3]);
     }
 }
 
