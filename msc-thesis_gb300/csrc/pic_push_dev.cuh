@@ -347,27 +347,30 @@ __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, 
     float ke = 0.f, px = 0.f, py = 0.f;
     bool bad = false;
     const long long lane4 = 4ll * (threadIdx.x & 31);
-    for (long long qw = base + 4ll * (threadIdx.x & ~31u); qw < end; qw += 4ll * blockDim.x) {
-        const long long q = qw + lane4;
-        const bool live = q < end;
-        int cc[4] = {-1, -1, -1, -1};
-        float xo[4] = {0.f, 0.f, 0.f, 0.f}, yo[4] = {0.f, 0.f, 0.f, 0.f};
-        float xv[4] = {0.f, 0.f, 0.f, 0.f}, yv[4] = {0.f, 0.f, 0.f, 0.f};
-        if (live) {
+    const long long stride = 4ll * blockDim.x;
+    {
+        for (long long qw = base + 4ll * (threadIdx.x & ~31u); qw < end; qw += stride) {
+            const long long q = qw + lane4;
+            const bool live = q < end;
             // plain (coherent) loads: with an in-place pass the same addresses are stored below
-            const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
-            const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
-            const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
-            const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
-            const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
-            cc[0] = c4.x, cc[1] = c4.y, cc[2] = c4.z, cc[3] = c4.w;
-            xo[0] = a4.x, xo[1] = a4.y, xo[2] = a4.z, xo[3] = a4.w;
-            yo[0] = b4.x, yo[1] = b4.y, yo[2] = b4.z, yo[3] = b4.w;
-            xv[0] = u4.x, xv[1] = u4.y, xv[2] = u4.z, xv[3] = u4.w;
-            yv[0] = v4.x, yv[1] = v4.y, yv[2] = v4.z, yv[3] = v4.w;
+            int cc[4] = {-1, -1, -1, -1};
+            float xo[4] = {0.f, 0.f, 0.f, 0.f}, yo[4] = {0.f, 0.f, 0.f, 0.f};
+            float xv[4] = {0.f, 0.f, 0.f, 0.f}, yv[4] = {0.f, 0.f, 0.f, 0.f};
+            if (live) {
+                const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
+                const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
+                const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
+                const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+                const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+                cc[0] = c4.x, cc[1] = c4.y, cc[2] = c4.z, cc[3] = c4.w;
+                xo[0] = a4.x, xo[1] = a4.y, xo[2] = a4.z, xo[3] = a4.w;
+                yo[0] = b4.x, yo[1] = b4.y, yo[2] = b4.z, yo[3] = b4.w;
+                xv[0] = u4.x, xv[1] = u4.y, xv[2] = u4.z, xv[3] = u4.w;
+                yv[0] = v4.x, yv[1] = v4.y, yv[2] = v4.z, yv[3] = v4.w;
+            }
+            push_quad<GATHER, DEPOSIT, AGG>(G, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+            if (live) store_quad(A, q, cc, xo, yo, xv, yv);
         }
-        push_quad<GATHER, DEPOSIT, AGG>(G, W, cc, xo, yo, xv, yv, ke, px, py, bad);
-        if (live) store_quad(A, q, cc, xo, yo, xv, yv);
     }
     finish_block<DEPOSIT>(G, W, sAcc, ke, px, py, bad);
 }

@@ -85,6 +85,13 @@ def test_results_independent_of_sort_cadence_and_graphs():
     a1, r1, f1 = run_state(cfg1, n, 15, seed=4)
     a2, r2, f2 = run_state(cfg2, n, 15, seed=4)
     a3, r3, f3 = run_state(cfg2, n, 15, seed=4, eager=True)
+    for variant in (3,):  # warp-summed deposit groups
+        cfgv, _, _ = normalized_electrons(nx, ny, 8.0, 4.0, n, 0.1, sort_every=7, chunk=512,
+                                          push_variant=variant)
+        av, rv, fv = run_state(cfgv, n, 15, seed=4)
+        for k in a1:
+            np.testing.assert_array_equal(a1[k], av[k], err_msg=f"variant {variant} {k}")
+        np.testing.assert_array_equal(r1, rv)
     for k in a1:
         np.testing.assert_array_equal(a1[k], a2[k], err_msg=k)
         np.testing.assert_array_equal(a2[k], a3[k], err_msg=k)
