@@ -231,12 +231,24 @@ def bench_ensemble(args):
     import torch
 
     import picgpu as P
+    import replicas as R
 
     rank, world, local = dist_env()
-    if rank != 0:
-        return
     torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
     cfgs, specs, grids, ppcs = c5_runs(P, nruns=args.runs, local=local)
+    total_all = sum(int(s.n) for s in specs)
+    grid_counts = {str(k): int((grids == k).sum()) for k in (64, 128, 256, 512)}
+    # the runs shard over ranks with no exchange: each rank advances its share
+    mine = R.shard_runs([int(s.n) for s in specs], world)[rank]
+    cfgs = [cfgs[i] for i in mine]
+    specs = [specs[i] for i in mine]
+    grids, ppcs = grids[mine], ppcs[mine]
     total = sum(int(s.n) for s in specs)
     tune = None
     if args.no_tune:
@@ -261,7 +273,10 @@ def bench_ensemble(args):
         clk = clocks.stop()
         charge_ok = all(E.diagnostics(r).total_charge_fixed == E.diagnostics(r).expected_charge_fixed
                         for r in range(len(cfgs)))
-    ens_value = total * args.steps / (ms / 1000.0)
+    if pg:
+        pg.barrier()
+    ms = R.max_over_ranks(ms, pg, device="cuda")
+    ens_value = R.whole_job_rate(total_all * args.steps, ms / 1000.0)
     S = int(cfgs[0].sort_every)
     _, _, since_w = launches_for(args.warmup, 0, S)
     nb1 = -(-sum(int(g) * int(g) + 1 for g in grids) // 4096)
@@ -289,7 +304,8 @@ def bench_ensemble(args):
             a1.record(st)
             h.synchronize()
             plain_ms += a0.elapsed_time(a1)
-    plain_value = total * args.steps / (plain_ms / 1000.0) if plain_ms else None
+    plain_ms = R.max_over_ranks(plain_ms, pg, device="cuda")
+    plain_value = R.whole_job_rate(total_all * args.steps, plain_ms / 1000.0) if plain_ms else None
     # forward + adjoint of every run (checkpoint every `every` steps, reversal
     # in between): particle-steps of the forward over the whole call's time
     adj = None
@@ -298,21 +314,27 @@ def bench_ensemble(args):
             E.adjoint(specs, 2 * args.every, args.every, gradients=False)  # warm-up (plans)
             t0 = time.perf_counter()
             res, _ = E.adjoint(specs, args.adjoint_steps, args.every, gradients=False)
-            el = time.perf_counter() - t0
-        adj = {"value": total * args.adjoint_steps / el, "unit": "particle-steps/s",
+            el = R.max_over_ranks(time.perf_counter() - t0, pg, device="cuda")
+        adj = {"value": R.whole_job_rate(total_all * args.adjoint_steps, el), "unit": "particle-steps/s",
                "steps": args.adjoint_steps, "every": args.every, "seconds": el,
                "note": "forward with checkpoints + reversed backward walk, one call",
                "J_run0": res[0][0], "dJ_dbeam_run0": res[0][1], "dJ_damp_run0": res[0][2]}
     cells = int(sum(int(g) * int(g) for g in grids))
-    step_bytes = BYTES_PER_PARTICLE * total + BYTES_PER_CELL * cells
+    step_bytes = BYTES_PER_PARTICLE * total + BYTES_PER_CELL * cells  # this rank's
     achieved = step_bytes * args.steps / (ms / 1000.0) / 1e9
+    if pg:
+        pg.destroy_process_group()
+    if rank != 0:
+        return
     print(json.dumps({
-        "metric": METRIC, "value": ens_value, "unit": "particle-steps/s", "n_gpus": 1,
+        "metric": METRIC, "value": ens_value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"ensemble-{len(cfgs)}-two-stream", "runs": len(cfgs), "particles": total,
-                   "cells": cells, "grid_counts": {str(k): int((grids == k).sum()) for k in (64, 128, 256, 512)},
+        "config": {"workload": f"ensemble-{args.runs}-two-stream", "runs": args.runs,
+                   "runs_rank0": len(cfgs), "particles": total_all,
+                   "cells": cells, "grid_counts": grid_counts,
+                   "parallelism": f"runs sharded over {world} ranks" if world > 1 else "single",
                    "chunk": int(cfgs[0].chunk), "sort_every": S, "sorts_in_timed_steps": ens_sorts,
                    "tune_ms_per_step": tune.ms_per_step if tune else None,
                    "charge_exact": charge_ok,
@@ -369,6 +391,7 @@ def main():
     import torch
 
     import picgpu as P
+    import replicas as R
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -418,12 +441,8 @@ def main():
     barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    ms_max = ms
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * N * args.steps / (ms_max / 1000.0)
+    ms_max = R.max_over_ranks(ms, pg, device="cuda")
+    value = R.whole_job_rate(world * N * args.steps, ms_max / 1000.0)
     diag = h.diagnostics()
 
     # dominant kernel (fused gather+push+deposit): eager launches timed with
@@ -456,12 +475,8 @@ def main():
         t0 = time.perf_counter()
         h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.steps, 1,
              *[x.data_ptr() for x in hout])
-        el = time.perf_counter() - t0
-        if pg:
-            t = torch.tensor([el], device="cuda")
-            pg.all_reduce(t, op=pg.ReduceOp.MAX)
-            el = float(t.item())
-        e2e = {"value": world * N * args.steps / el, "unit": "particle-steps/s",
+        el = R.max_over_ranks(time.perf_counter() - t0, pg, device="cuda")
+        e2e = {"value": R.whole_job_rate(world * N * args.steps, el), "unit": "particle-steps/s",
                "h2d_bytes_per_step": 32 * N / args.steps, "d2h_bytes_per_step": 32 * N / args.steps,
                "seconds": el, "steps": args.steps}
         del hin, hout
