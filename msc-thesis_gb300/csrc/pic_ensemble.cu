@@ -754,8 +754,24 @@ pic_status pic_ensemble_init(pic_ensemble *e, const pic_init_spec *specs)
     PIC_CUDA(cudaMemcpyAsync(e->dev, z.data(), sizeof(DevState) * z.size(), cudaMemcpyHostToDevice, st));
     PIC_CUDA(cudaMemsetAsync(e->hist, 0, sizeof(double) * 6 * e->hist_cap * (size_t)e->nruns, st));
     PIC_CUDA(cudaMemsetAsync(e->rho_fix, 0, 8 * (size_t)e->nnodes, st));
-    // sort into buffer 1, deposit while copying back, solve, prime
-    PIC_TRY(ens_sort(e));
+    // radix sort of the loads into buffer 1, deposit while copying back,
+    // solve, prime
+    {
+        uint32_t *scratch = nullptr;
+        void *temp = nullptr;
+        size_t temp_bytes = 0;
+        PIC_CUDA(cudaMalloc(&scratch, 16 * ns));
+        pic_status s_ = ens_import_sort(e, scratch, &temp, &temp_bytes);
+        if (s_ == PIC_OK && e->npush) {
+            ens_anchor_kernel<<<(e->npush + 255) / 256, 256, 0, st>>>(e->cell[1], e->push_blk,
+                                                                      e->d_runs, e->npush, e->anchor);
+            if (cudaGetLastError() != cudaSuccess) s_ = PIC_ERR_CUDA;
+        }
+        cudaStreamSynchronize(st);
+        cudaFree(scratch);
+        if (temp) cudaFree(temp);
+        PIC_TRY(s_);
+    }
     PIC_TRY(ens_launch_push(e, 1, 2));
     PIC_TRY(ens_poisson(e));
     PIC_TRY(ens_launch_push(e, 0, 1));

@@ -104,6 +104,7 @@ static void free_handle_buffers(pic_handle *h)
     if (h->g_period) cudaGraphExecDestroy(h->g_period);
     if (h->g_sortstep) cudaGraphExecDestroy(h->g_sortstep);
     if (h->g_one) cudaGraphExecDestroy(h->g_one);
+    if (h->cub_temp) cudaFree(h->cub_temp);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -281,11 +282,13 @@ static pic_status copy_back(pic_handle *h, int s)
     return PIC_OK;
 }
 
-static pic_status sort_now(pic_handle *h)
+// import: arbitrary order, radix sort of the keys (pic_import.cu);
+// otherwise the periodic counting sort
+static pic_status sort_now(pic_handle *h, bool import = false)
 {
     for (int s = 0; s < h->cfg.nspecies; ++s) {
         if (!h->sp[s].cap) continue;
-        PIC_TRY(launch_sort(h, s));
+        PIC_TRY(import ? import_sort(h, s) : launch_sort(h, s));
         PIC_TRY(copy_back(h, s));
     }
     h->since_sort = 0;
@@ -305,7 +308,7 @@ pic_status deposit_now(pic_handle *h)
 pic_status refresh(pic_handle *h)
 {
     update_mean(h);
-    PIC_TRY(sort_now(h));
+    PIC_TRY(sort_now(h, true));
     PIC_TRY(deposit_now(h));
     PIC_TRY(record_poisson(h));
     PIC_CUDA(cudaStreamSynchronize(h->stream));

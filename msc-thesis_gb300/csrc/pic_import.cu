@@ -1,0 +1,163 @@
+// pic_import.cu -- sorting particles that arrive in arbitrary order.
+//
+// The periodic counting sort (pic_sort.cu) relies on the previous order:
+// a block's keys fall in a short range.  After an import (host arrays,
+// a random load, a state file) the order is arbitrary, and that sort
+// degenerates to one global atomic and one scattered store per field and
+// particle.  Here the cell keys are sorted as (key, slot) pairs with the
+// CUDA toolkit's radix sort (CUB, a library sort of 32-bit pairs over the
+// key's significant bits only) and the particle fields are then gathered
+// into buffer 1 in key order.  Runs once per import, never in the step.
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "pic_ensemble.cuh"
+#include "pic_internal.cuh"
+#include "pic_sort_dev.cuh"
+
+namespace pic {
+
+__global__ void import_keys_kernel(const int32_t *__restrict__ cell, long long n, KeyGeo G,
+                                   unsigned *err, uint32_t *__restrict__ keys,
+                                   uint32_t *__restrict__ idx)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        keys[i] = (uint32_t)particle_key(G, err, cell[i]);
+        idx[i] = (uint32_t)i;
+    }
+}
+
+// ensemble: every slot of every run, keys in the shared key space
+__global__ void import_keys_ens_kernel(const int32_t *__restrict__ cell,
+                                       const SegBlock *__restrict__ blk,
+                                       const EnsRun *__restrict__ runs, unsigned *err,
+                                       uint32_t *__restrict__ keys, uint32_t *__restrict__ idx)
+{
+    const SegBlock b = blk[blockIdx.x];
+    const EnsRun &R = runs[b.run];
+    const KeyGeo G{R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off};
+    for (long long i = b.base + threadIdx.x; i < b.base + b.count; i += blockDim.x) {
+        keys[i] = (uint32_t)particle_key(G, err, cell[i]);
+        idx[i] = (uint32_t)i;
+    }
+}
+
+struct Fields {
+    const uint32_t *in[7];
+    uint32_t *out[7];
+    int nf;
+};
+
+// out_f[i] = in_f[src[i]]
+__global__ void import_gather_kernel(Fields F, const uint32_t *__restrict__ src, long long n)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t j = src[i];
+#pragma unroll
+        for (int f = 0; f < 7; ++f)
+            if (f < F.nf) F.out[f][i] = F.in[f][j];
+    }
+}
+
+namespace {
+
+int key_bits(long long nkeys)
+{
+    int b = 1;
+    while ((1ll << b) < nkeys) ++b;
+    return b;
+}
+
+// (key, slot) radix sort in `scratch` (4 arrays of n words) plus CUB's
+// temporary storage (grown on demand in *temp / *temp_bytes)
+pic_status radix_pairs(uint32_t *scratch, long long n, int bits, void **temp, size_t *temp_bytes,
+                       cudaStream_t st, const uint32_t **sorted_idx)
+{
+    uint32_t *k0 = scratch, *k1 = scratch + n, *v0 = scratch + 2 * n, *v1 = scratch + 3 * n;
+    cub::DoubleBuffer<uint32_t> keys(k0, k1), vals(v0, v1);
+    size_t need = 0;
+    PIC_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, need, keys, vals, (int)n, 0, bits, st));
+    if (need > *temp_bytes) {
+        if (*temp) cudaFree(*temp);
+        *temp = nullptr;
+        *temp_bytes = 0;
+        PIC_CUDA(cudaMalloc(temp, need));
+        *temp_bytes = need;
+    }
+    PIC_CUDA(cub::DeviceRadixSort::SortPairs(*temp, need, keys, vals, (int)n, 0, bits, st));
+    *sorted_idx = vals.Current();
+    return PIC_OK;
+}
+
+}  // namespace
+
+// Species s of a handle, live in buffer 0 in arbitrary order -> buffer 1 in
+// key order (the caller copies back), anchors from buffer 1.
+pic_status import_sort(pic_handle *h, int s)
+{
+    SpeciesBuf &B = h->sp[s];
+    const long long n = B.cap;  // padding slots (cell -1) sort to the end
+    if (!n) return PIC_OK;
+    if (n >= (1ll << 31)) {
+        set_error("import sort: more than 2^31 slots");
+        return PIC_ERR_INVALID_ARG;
+    }
+    const Geometry &g = h->g;
+    PIC_TRY(ensure_stage(h, (size_t)n * 16));
+    uint32_t *scratch = (uint32_t *)h->stage;
+    const KeyGeo G{g.nx, g.ny, g.tw, g.th, g.ntx, 0};
+    import_keys_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(B.cell[0], n, G, &h->dev->err,
+                                                                scratch, scratch + 2 * n);
+    PIC_CUDA(cudaGetLastError());
+    const uint32_t *idx = nullptr;
+    PIC_TRY(radix_pairs(scratch, n, key_bits((long long)g.nx * g.ny + 1), &h->cub_temp,
+                        &h->cub_temp_bytes, h->stream, &idx));
+    Fields F;
+    memset(&F, 0, sizeof F);
+    const void *in[7] = {B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.pid[0], B.vz[0]};
+    void *out[7] = {B.cell[1], B.ox[1], B.oy[1], B.vx[1], B.vy[1], B.pid[1], B.vz[1]};
+    F.nf = B.vz[0] ? 7 : 6;
+    for (int f = 0; f < F.nf; ++f) {
+        F.in[f] = (const uint32_t *)in[f];
+        F.out[f] = (uint32_t *)out[f];
+    }
+    import_gather_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(F, idx, n);
+    PIC_CUDA(cudaGetLastError());
+    return launch_anchors(h, s);
+}
+
+// Every run of an ensemble: buffer 0 in arbitrary order -> buffer 1 in key
+// order (anchors are the caller's).
+pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, void **temp, size_t *temp_bytes)
+{
+    const long long n = E->nslots;
+    if (n >= (1ll << 31)) {
+        set_error("import sort: more than 2^31 slots");
+        return PIC_ERR_INVALID_ARG;
+    }
+    cudaStream_t st = E->stream;
+    import_keys_ens_kernel<<<E->nsort, 256, 0, st>>>(E->cell[0], E->sort_blk, E->d_runs,
+                                                      &E->dev[0].err, scratch, scratch + 2 * n);
+    PIC_CUDA(cudaGetLastError());
+    const uint32_t *idx = nullptr;
+    PIC_TRY(radix_pairs(scratch, n, key_bits(E->nkeys), temp, temp_bytes, st, &idx));
+    Fields F;
+    memset(&F, 0, sizeof F);
+    const void *in[6] = {E->cell[0], E->ox[0], E->oy[0], E->vx[0], E->vy[0], E->pid[0]};
+    void *out[6] = {E->cell[1], E->ox[1], E->oy[1], E->vx[1], E->vy[1], E->pid[1]};
+    F.nf = 6;
+    for (int f = 0; f < 6; ++f) {
+        F.in[f] = (const uint32_t *)in[f];
+        F.out[f] = (uint32_t *)out[f];
+    }
+    import_gather_kernel<<<grid_for(n, 256), 256, 0, st>>>(F, idx, n);
+    PIC_CUDA(cudaGetLastError());
+    return PIC_OK;
+}
+
+}  // namespace pic

@@ -180,6 +180,9 @@ struct pic_handle {
     pic::DsmcState dsmc;
     // push kernel variant: bulk-copy pipeline (chunk a multiple of its stage)
     bool use_bulk = false;
+    // radix sort temporary storage of the import sort
+    void *cub_temp = nullptr;
+    size_t cub_temp_bytes = 0;
 };
 
 namespace pic {
@@ -197,6 +200,9 @@ pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s);
 pic_status scatter_smem_attr(const void *kernel);
+pic_status launch_anchors(pic_handle *h, int s);
+// pic_import.cu: arbitrary order in buffer 0 -> key order in buffer 1 (+ anchors)
+pic_status import_sort(pic_handle *h, int s);
 // exclusive scan of count[0, nkeys) into offset and cursor, offset[nkeys] =
 // *d_total; bsum, bsum_s: ceil(nkeys / 4096) entries, bsum2: ceil(that / 4096)
 pic_status launch_key_scan(const uint32_t *count, uint32_t *offset, uint32_t *cursor,

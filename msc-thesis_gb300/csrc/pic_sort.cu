@@ -196,6 +196,29 @@ pic_status scatter_smem_attr(const void *kernel)
     return PIC_OK;
 }
 
+// Chunk anchors of species s from the sorted order in buffer 1.
+pic_status launch_anchors(pic_handle *h, int s)
+{
+    SpeciesBuf &B = h->sp[s];
+    const Geometry &g = h->g;
+    if (!B.nchunks) return PIC_OK;
+    SortArgs A;
+    memset(&A, 0, sizeof A);
+    A.cout = B.cell[1];
+    A.anchor = B.anchor;
+    A.d_n = &h->dev->n[s];
+    A.nx = g.nx;
+    A.ny = g.ny;
+    A.tw = g.tw;
+    A.th = g.th;
+    A.ntx = g.ntx;
+    A.chunk = g.chunk;
+    PIC_CUDA(cudaMemsetAsync(B.anchor, 0xFF, sizeof(int32_t) * (size_t)B.nchunks, h->stream));
+    sort_anchor_kernel<<<(unsigned)((B.nchunks + 255) / 256), 256, 0, h->stream>>>(A, B.nchunks);
+    PIC_CUDA(cudaGetLastError());
+    return PIC_OK;
+}
+
 // Sort species s from buffer 0 into buffer 1 and compute the chunk anchors.
 pic_status launch_sort(pic_handle *h, int s)
 {
