@@ -382,6 +382,19 @@ static pic_status need_species(pic_handle *h, int s)
     return PIC_OK;
 }
 
+// Device address of a page-locked host array (allocated or registered with
+// the CUDA runtime), or null for other memory.
+template <class T> static T *mapped(T *p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? (T *)a.devicePointer : nullptr;
+}
+
 pic_status ensure_stage(pic_handle *h, size_t bytes)
 {
     if (h->stage_bytes >= bytes) return PIC_OK;
@@ -659,17 +672,26 @@ pic_status pic_set_particles(pic_handle *h, int s, long long n, const double *x,
         return PIC_ERR_INVALID_ARG;
     }
     const size_t nn = (size_t)n;
-    PIC_TRY(ensure_stage(h, std::max<size_t>(1, nn) * 5 * sizeof(double)));
-    double *d = (double *)h->stage;
-    if (n) {
-        PIC_CUDA(cudaMemcpyAsync(d, x, nn * 8, cudaMemcpyHostToDevice, h->stream));
-        PIC_CUDA(cudaMemcpyAsync(d + nn, y, nn * 8, cudaMemcpyHostToDevice, h->stream));
-        PIC_CUDA(cudaMemcpyAsync(d + 2 * nn, vx, nn * 8, cudaMemcpyHostToDevice, h->stream));
-        PIC_CUDA(cudaMemcpyAsync(d + 3 * nn, vy, nn * 8, cudaMemcpyHostToDevice, h->stream));
-        if (vz) PIC_CUDA(cudaMemcpyAsync(d + 4 * nn, vz, nn * 8, cudaMemcpyHostToDevice, h->stream));
-    }
     PIC_TRY(set_count(h, s, n));
-    PIC_TRY(launch_from_global(h, s, n, d, d + nn, d + 2 * nn, d + 3 * nn, vz ? d + 4 * nn : nullptr));
+    const double *dx = mapped(x), *dy = mapped(y), *dvx = mapped(vx), *dvy = mapped(vy);
+    const double *dvz = vz ? mapped(vz) : nullptr;
+    if (n && dx && dy && dvx && dvy && (!vz || dvz)) {
+        // page-locked host arrays: the conversion kernel reads them in place
+        // over the CPU-GPU link (coalesced, in particle order)
+        PIC_TRY(launch_from_global(h, s, n, dx, dy, dvx, dvy, dvz));
+    } else {
+        PIC_TRY(ensure_stage(h, std::max<size_t>(1, nn) * 5 * sizeof(double)));
+        double *d = (double *)h->stage;
+        if (n) {
+            PIC_CUDA(cudaMemcpyAsync(d, x, nn * 8, cudaMemcpyHostToDevice, h->stream));
+            PIC_CUDA(cudaMemcpyAsync(d + nn, y, nn * 8, cudaMemcpyHostToDevice, h->stream));
+            PIC_CUDA(cudaMemcpyAsync(d + 2 * nn, vx, nn * 8, cudaMemcpyHostToDevice, h->stream));
+            PIC_CUDA(cudaMemcpyAsync(d + 3 * nn, vy, nn * 8, cudaMemcpyHostToDevice, h->stream));
+            if (vz) PIC_CUDA(cudaMemcpyAsync(d + 4 * nn, vz, nn * 8, cudaMemcpyHostToDevice, h->stream));
+        }
+        PIC_TRY(launch_from_global(h, s, n, d, d + nn, d + 2 * nn, d + 3 * nn,
+                                   vz ? d + 4 * nn : nullptr));
+    }
     PIC_TRY(reset_device_state(h));
     return refresh(h);
 }
