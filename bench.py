@@ -350,6 +350,130 @@ def bench_ensemble(args):
         "gpu_launches": ens_launches, "clocks": clk}), flush=True)
 
 
+# SI constants of the collisional workloads (configs 3 and 4)
+E_CH, M_E, K_B = 1.602176634e-19, 9.1093837015e-31, 1.380649e-23
+M_I = 73000.0 * M_E
+N_GAS = 3.2e21
+T_GAS_EV = K_B * 300.0 / E_CH
+EPS0_SI = 8.8541878128e-12
+
+
+def c3_tables(ntab=256, emin=0.01, emax=1000.0):
+    """256 log-spaced energies 0.01..1000 eV: elastic 5e-20 m^2; excitation
+    11.5 eV rising linearly to 2e-20 at 30 eV, then flat; ionisation 15.8 eV
+    rising linearly to 3e-20 at 100 eV, then flat."""
+    import numpy as np
+
+    e = emin * (emax / emin) ** (np.arange(ntab) / (ntab - 1))
+    sel = np.full(ntab, 5e-20)
+    sexc = np.where(e < 11.5, 0.0, np.where(e < 30.0, 2e-20 * (e - 11.5) / 18.5, 2e-20))
+    sion = np.where(e < 15.8, 0.0, np.where(e < 100.0, 3e-20 * (e - 15.8) / 84.2, 3e-20))
+    return sel, sexc, sion
+
+
+def small_workload(P, kind, local):
+    """Handles of the other configurations, loaded and primed:
+    c1    two-stream, 128^2, 100 ppc, beams +-0.2, vth 0.01, x-displacement
+          1e-3 in k = 0.5, dt 0.1 (plasma units)
+    mcc   512^2, 64 electrons + 64 ions per cell (mass ratio 1/73,000),
+          n_e 1e15 m^-3, dx 2e-4 m, Te 2 eV, null-collision MCC against
+          3.2e21 m^-3 neutrals at 300 K, dt 1e-11 s
+    dsmc  the mcc workload plus 50 hard-sphere neutrals per cell (6.6e-26 kg,
+          d 3.6e-10 m), bimodal 300 K / 1000 K, Bird NTC every step
+    Returns (handle, particles pushed per step, cells, description)."""
+    import numpy as np
+
+    if kind == "c1":
+        nx, ppc = 128, 100
+        n = nx * nx * ppc
+        L = 4 * np.pi
+        A = L * L
+        cfg = P.config(nx, nx, L, L, 0.1, [P.species(n, -A / n, A / n, -1)], device=local)
+        h = P.Handle(cfg)
+        h.init_particles(0, P.init_spec(n, vth=(0.01, 0.01, 0.0), beam_v=0.2,
+                                        pert_kind=P.PERT_XDISP, pert_amp=1e-3, pert_mx=1, seed=0))
+        h.prime_leapfrog()
+        return h, n, nx * nx, "two-stream-128x128-100ppc"
+    nx = 512
+    dx = 2e-4
+    L = nx * dx
+    ne = nx * nx * 64
+    w = 1e15 * L * L / ne
+    sp = [P.species(ne + ne // 4, -E_CH * w, M_E * w, -1, P.SPECIES_HAS_VZ),
+          P.species(ne + ne // 4, E_CH * w, M_I * w, 1, P.SPECIES_HAS_VZ)]
+    nn = nx * nx * 50
+    wn = N_GAS * L * L / nn
+    if kind == "dsmc":
+        sp.append(P.species(nn, 0.0, 6.6e-26 * wn, 0, P.SPECIES_HAS_VZ))
+    cfg = P.config(nx, nx, L, L, 1e-11, sp, eps0=EPS0_SI, device=local)
+    h = P.Handle(cfg)
+    ve, vi = np.sqrt(2.0 * E_CH / M_E), np.sqrt(T_GAS_EV * E_CH / M_I)
+    h.init_particles(0, P.init_spec(ne, vth=(ve, ve, ve), seed=5))
+    h.init_particles(1, P.init_spec(ne, vth=(vi, vi, vi), seed=6))
+    sel, sexc, sion = c3_tables()
+    h.set_mcc(0, 1, N_GAS, T_GAS_EV, M_E, M_I, E_CH, 0.01, 1000.0, sel, sexc, sion, 11.5,
+              15.8, 9)
+    pushed = 2 * ne
+    if kind == "dsmc":
+        rng = np.random.default_rng(1)
+        x, y = rng.random(nn) * L, rng.random(nn) * L
+        t = np.where(np.arange(nn) % 2 == 0, 300.0, 1000.0)
+        s = np.sqrt(K_B * t / 6.6e-26)
+        v = rng.normal(size=(3, nn)) * s
+        h.set_particles(2, x, y, v[0], v[1], v[2])
+        h.set_dsmc(2, 3.6e-10, wn, 1.0, np.pi * (3.6e-10) ** 2 * 3000.0, 21)
+        pushed += nn
+    h.prime_leapfrog()
+    desc = "mcc-512x512-64e64i" if kind == "mcc" else "dsmc-512x512-64e64i50n"
+    return h, pushed, nx * nx, desc
+
+
+def bench_small(args):
+    """One GPU, one of the other configurations: particle-steps/s of the whole
+    step (all pushed species, collisions included) with the particles resident."""
+    import torch
+
+    import picgpu as P
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    h, n, cells, desc = small_workload(P, args.workload, local)
+    stream = torch.cuda.ExternalStream(h.stream())
+    h.step(args.warmup)
+    h.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    h.step(args.steps)
+    e1.record(stream)
+    h.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    d = h.diagnostics()
+    counts = [int(c) for c in h.collision_counts()] if args.workload != "c1" else None
+    h.close()
+    hbm, peak_kind = peaks()
+    step_bytes = BYTES_PER_PARTICLE * n + BYTES_PER_CELL * cells
+    achieved = step_bytes * args.steps / (ms / 1000.0) / 1e9
+    print(json.dumps({
+        "metric": METRIC, "value": n * args.steps / (ms / 1000.0), "unit": "particle-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": desc, "particles_pushed_per_step": n, "cells": cells,
+                   "charge_exact": d.total_charge_fixed == d.expected_charge_fixed,
+                   "error_flags": d.error_flags, "collision_counts": counts,
+                   "peak_kind": peak_kind},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "kernel": "whole step, 40 B per pushed particle + 60 B per cell"},
+        "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": clk}), flush=True)
+
+
 def main():
     global NX, NY, N, L, SORT_EVERY
     ap = argparse.ArgumentParser()
@@ -371,8 +495,11 @@ def main():
     ap.add_argument("--runs", type=int, default=64, help="ensemble workload: runs (profiling on fewer)")
     ap.add_argument("--no-plain", action="store_true",
                     help="ensemble workload: skip the one-run-at-a-time comparison")
-    ap.add_argument("--workload", default="landau", choices=["landau", "ensemble"],
-                    help="landau: the 2048^2 run (default); ensemble: 64 batched two-stream runs")
+    ap.add_argument("--workload", default="landau",
+                    choices=["landau", "ensemble", "c1", "mcc", "dsmc"],
+                    help="landau: the 2048^2 run (default); ensemble: 64 batched two-stream "
+                         "runs; c1: 128^2 two-stream; mcc: 512^2 electrons + ions with MCC; "
+                         "dsmc: mcc plus DSMC neutrals")
     args = ap.parse_args()
     NX = NY = args.nx
     N = NX * NY * PPC
@@ -385,6 +512,9 @@ def main():
         return
     if args.workload == "ensemble":
         bench_ensemble(args)
+        return
+    if args.workload in ("c1", "mcc", "dsmc"):
+        bench_small(args)
         return
 
     import numpy as np
