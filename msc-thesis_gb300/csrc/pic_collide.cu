@@ -89,11 +89,117 @@ __device__ __forceinline__ void mcc_sigmas(const MccArgs &A, const float *tab, f
     sion = fmaf(f, io[k + 1] - io[k], io[k]);
 }
 
+constexpr int MCC_CHUNK = 2048;  // electrons tested per block pass
+
+// Collision of candidate electron i (r: its first draw of this pass):
+// real (elastic, excitation, ionisation with ion birth) or null.
+__device__ __forceinline__ void mcc_collide(const MccArgs &A, const float *s_tab, long long i,
+                                            uint32_t pid, unsigned long long pass, const U4 &r,
+                                            unsigned &c_el, unsigned &c_exc, unsigned &c_ion,
+                                            unsigned &c_null, bool &overflow)
+{
+    float vx = A.evx[i], vy = A.evy[i], vz = A.evz[i];
+    const float v2 = vx * vx + vy * vy + vz * vz;
+    const float v = sqrtf(v2);
+    const float E = A.half_me_over_e * v2;
+    float sel, sexc, sion;
+    mcc_sigmas(A, s_tab, E, sel, sexc, sion);
+    if (E < A.e_exc) sexc = 0.f;
+    if (E < A.e_ion) sion = 0.f;
+    const float nu_el = A.ng * sel * v, nu_exc = A.ng * sexc * v, nu_ion = A.ng * sion * v;
+    const float R = u01f(r.y) * A.nu_max;
+    const float ux = v > 0.f ? vx / v : 0.f, uy = v > 0.f ? vy / v : 0.f;
+    const float uz = v > 0.f ? vz / v : 1.f;
+    if (R < nu_el) {
+        const float c = 1.f - 2.f * u01f(r.z);
+        const float En = E * (1.f - A.two_m_over_M * (1.f - c));
+        const float3 d = deflect(ux, uy, uz, c, u01f(r.w));
+        const float vn = sqrtf(En / A.half_me_over_e);
+        vx = vn * d.x;
+        vy = vn * d.y;
+        vz = vn * d.z;
+        ++c_el;
+    } else if (R < nu_el + nu_exc) {
+        const float c = 1.f - 2.f * u01f(r.z);
+        const float3 d = deflect(ux, uy, uz, c, u01f(r.w));
+        const float vn = sqrtf(fmaxf(E - A.e_exc, 0.f) / A.half_me_over_e);
+        vx = vn * d.x;
+        vy = vn * d.y;
+        vz = vn * d.z;
+        ++c_exc;
+    } else if (R < nu_el + nu_exc + nu_ion) {
+        const U4 r2 = philox4x32_10(U4{pid, (uint32_t)pass, 1u, STREAM_MCC}, A.k0, A.k1);
+        const float Er = fmaxf(E - A.e_ion, 0.f);
+        const float Ej = u01f(r2.x) * Er, Es = Er - Ej;
+        const float3 ds = deflect(ux, uy, uz, 1.f - 2.f * u01f(r.z), u01f(r.w));
+        const float3 dj = deflect(ux, uy, uz, 1.f - 2.f * u01f(r2.y), u01f(r2.z));
+        const float vs = sqrtf(Es / A.half_me_over_e), vj = sqrtf(Ej / A.half_me_over_e);
+        vx = vs * ds.x;
+        vy = vs * ds.y;
+        vz = vs * ds.z;
+        ++c_ion;
+        if (A.has_ion) {
+            // reserve the ion slot, then the electron slot; a reservation past
+            // the capacity is given back, so the successful slots stay
+            // contiguous from the old count
+            const long long ji = (long long)atomicAdd((unsigned long long *)A.d_ni, 1ull);
+            long long je = A.ecap;
+            if (ji < A.icap) je = (long long)atomicAdd((unsigned long long *)A.d_ne, 1ull);
+            if (ji < A.icap && je < A.ecap) {
+                A.ecell[je] = A.ecell[i];
+                A.eox[je] = A.eox[i];
+                A.eoy[je] = A.eoy[i];
+                A.evx[je] = vj * dj.x;
+                A.evy[je] = vj * dj.y;
+                A.evz[je] = vj * dj.z;
+                A.epid[je] = (uint32_t)je;
+                const U4 r3 = philox4x32_10(U4{pid, (uint32_t)pass, 2u, STREAM_MCC}, A.k0, A.k1);
+                const float ra = sqrtf(-2.f * __logf(u01f(r3.x))), rb = sqrtf(-2.f * __logf(u01f(r3.z)));
+                float sa, ca, sb, cb;
+                sincospif(2.f * u01f(r3.y), &sa, &ca);
+                sincospif(2.f * u01f(r3.w), &sb, &cb);
+                A.icell[ji] = A.ecell[i];
+                A.iox[ji] = A.eox[i];
+                A.ioy[ji] = A.eoy[i];
+                A.ivx[ji] = A.vth_ion * ra * ca;
+                A.ivy[ji] = A.vth_ion * ra * sa;
+                A.ivz[ji] = A.vth_ion * rb * cb;
+                A.ipid[ji] = (uint32_t)ji;
+            } else {
+                // no room: give back what was reserved and report; an ion slot
+                // whose electron did not fit stays empty (cell -1)
+                if (ji >= A.icap) {
+                    atomicAdd((unsigned long long *)A.d_ni, (unsigned long long)-1ll);
+                } else {
+                    atomicAdd((unsigned long long *)A.d_ne, (unsigned long long)-1ll);
+                    A.icell[ji] = -1;
+                    A.ipid[ji] = (uint32_t)ji;
+                }
+                overflow = true;
+            }
+        }
+    } else {
+        ++c_null;
+        return;
+    }
+    A.evx[i] = vx;
+    A.evy[i] = vy;
+    A.evz[i] = vz;
+}
+
+// One null-collision pass over the electrons present at its start.  Each
+// block takes MCC_CHUNK electrons at a time: first every electron draws its
+// candidate test (one Philox draw keyed by particle id and pass) and the
+// candidates (fraction P_null, a few percent) are queued in shared memory,
+// then the block's threads work through the queue together, so the costly
+// collision path runs in full warps instead of one lane per warp.
 __global__ void __launch_bounds__(256) mcc_kernel(MccArgs A)
 {
-    extern __shared__ float s_tab[];
+    extern __shared__ float s_tab[];  // 4 ntab table floats, then the candidate queue
+    int *s_q = reinterpret_cast<int *>(s_tab + 4 * A.ntab);
     for (int i = threadIdx.x; i < 4 * A.ntab; i += blockDim.x) s_tab[i] = A.tab[i];
     __shared__ unsigned long long s_cnt[4];
+    __shared__ unsigned s_nq;
     if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0ull;
     __syncthreads();
     // the count at the start of the pass: electrons born in this pass are not
@@ -102,99 +208,36 @@ __global__ void __launch_bounds__(256) mcc_kernel(MccArgs A)
     const unsigned long long pass = A.dev->mcc_pass;
     unsigned c_el = 0, c_exc = 0, c_ion = 0, c_null = 0;
     bool overflow = false;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (A.ecell[i] < 0) continue;
-        const uint32_t pid = A.epid[i];
-        const U4 r = philox4x32_10(U4{pid, (uint32_t)pass, 0u, STREAM_MCC}, A.k0, A.k1);
-        if (u01f(r.x) >= A.p_null) continue;
-        float vx = A.evx[i], vy = A.evy[i], vz = A.evz[i];
-        const float v2 = vx * vx + vy * vy + vz * vz;
-        const float v = sqrtf(v2);
-        const float E = A.half_me_over_e * v2;
-        float sel, sexc, sion;
-        mcc_sigmas(A, s_tab, E, sel, sexc, sion);
-        if (E < A.e_exc) sexc = 0.f;
-        if (E < A.e_ion) sion = 0.f;
-        const float nu_el = A.ng * sel * v, nu_exc = A.ng * sexc * v, nu_ion = A.ng * sion * v;
-        const float R = u01f(r.y) * A.nu_max;
-        const float ux = v > 0.f ? vx / v : 0.f, uy = v > 0.f ? vy / v : 0.f;
-        const float uz = v > 0.f ? vz / v : 1.f;
-        if (R < nu_el) {
-            const float c = 1.f - 2.f * u01f(r.z);
-            const float En = E * (1.f - A.two_m_over_M * (1.f - c));
-            const float3 d = deflect(ux, uy, uz, c, u01f(r.w));
-            const float vn = sqrtf(En / A.half_me_over_e);
-            vx = vn * d.x;
-            vy = vn * d.y;
-            vz = vn * d.z;
-            ++c_el;
-        } else if (R < nu_el + nu_exc) {
-            const float c = 1.f - 2.f * u01f(r.z);
-            const float3 d = deflect(ux, uy, uz, c, u01f(r.w));
-            const float vn = sqrtf(fmaxf(E - A.e_exc, 0.f) / A.half_me_over_e);
-            vx = vn * d.x;
-            vy = vn * d.y;
-            vz = vn * d.z;
-            ++c_exc;
-        } else if (R < nu_el + nu_exc + nu_ion) {
-            const U4 r2 = philox4x32_10(U4{pid, (uint32_t)pass, 1u, STREAM_MCC}, A.k0, A.k1);
-            const float Er = fmaxf(E - A.e_ion, 0.f);
-            const float Ej = u01f(r2.x) * Er, Es = Er - Ej;
-            const float3 ds = deflect(ux, uy, uz, 1.f - 2.f * u01f(r.z), u01f(r.w));
-            const float3 dj = deflect(ux, uy, uz, 1.f - 2.f * u01f(r2.y), u01f(r2.z));
-            const float vs = sqrtf(Es / A.half_me_over_e), vj = sqrtf(Ej / A.half_me_over_e);
-            vx = vs * ds.x;
-            vy = vs * ds.y;
-            vz = vs * ds.z;
-            ++c_ion;
-            if (A.has_ion) {
-                // reserve the ion slot, then the electron slot; a reservation past
-                // the capacity is given back, so the successful slots stay
-                // contiguous from the old count
-                const long long ji = (long long)atomicAdd((unsigned long long *)A.d_ni, 1ull);
-                long long je = A.ecap;
-                if (ji < A.icap) je = (long long)atomicAdd((unsigned long long *)A.d_ne, 1ull);
-                if (ji < A.icap && je < A.ecap) {
-                    A.ecell[je] = A.ecell[i];
-                    A.eox[je] = A.eox[i];
-                    A.eoy[je] = A.eoy[i];
-                    A.evx[je] = vj * dj.x;
-                    A.evy[je] = vj * dj.y;
-                    A.evz[je] = vj * dj.z;
-                    A.epid[je] = (uint32_t)je;
-                    const U4 r3 = philox4x32_10(U4{pid, (uint32_t)pass, 2u, STREAM_MCC}, A.k0, A.k1);
-                    const float ra = sqrtf(-2.f * __logf(u01f(r3.x))), rb = sqrtf(-2.f * __logf(u01f(r3.z)));
-                    float sa, ca, sb, cb;
-                    sincospif(2.f * u01f(r3.y), &sa, &ca);
-                    sincospif(2.f * u01f(r3.w), &sb, &cb);
-                    A.icell[ji] = A.ecell[i];
-                    A.iox[ji] = A.eox[i];
-                    A.ioy[ji] = A.eoy[i];
-                    A.ivx[ji] = A.vth_ion * ra * ca;
-                    A.ivy[ji] = A.vth_ion * ra * sa;
-                    A.ivz[ji] = A.vth_ion * rb * cb;
-                    A.ipid[ji] = (uint32_t)ji;
-                } else {
-                    // no room: give back what was reserved and report; an ion slot
-                    // whose electron did not fit stays empty (cell -1)
-                    if (ji >= A.icap) {
-                        atomicAdd((unsigned long long *)A.d_ni, (unsigned long long)-1ll);
-                    } else {
-                        atomicAdd((unsigned long long *)A.d_ne, (unsigned long long)-1ll);
-                        A.icell[ji] = -1;
-                        A.ipid[ji] = (uint32_t)ji;
-                    }
-                    overflow = true;
-                }
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (long long c0 = (long long)blockIdx.x * MCC_CHUNK; c0 < n;
+         c0 += (long long)gridDim.x * MCC_CHUNK) {
+        if (threadIdx.x == 0) s_nq = 0u;
+        __syncthreads();
+        for (int k = threadIdx.x; k < MCC_CHUNK; k += blockDim.x) {  // same trip count in a warp
+            const long long i = c0 + k;
+            bool cand = false;
+            if (i < n && A.ecell[i] >= 0) {
+                const U4 r = philox4x32_10(U4{A.epid[i], (uint32_t)pass, 0u, STREAM_MCC}, A.k0, A.k1);
+                cand = u01f(r.x) < A.p_null;
             }
-        } else {
-            ++c_null;
-            continue;
+            const unsigned m = __ballot_sync(full, cand);
+            if (m) {
+                unsigned base = 0u;
+                if (lane == 0) base = atomicAdd(&s_nq, (unsigned)__popc(m));
+                base = __shfl_sync(full, base, 0);
+                if (cand) s_q[base + __popc(m & ((1u << lane) - 1u))] = k;
+            }
         }
-        A.evx[i] = vx;
-        A.evy[i] = vy;
-        A.evz[i] = vz;
+        __syncthreads();
+        const int nq = (int)s_nq;
+        for (int j = threadIdx.x; j < nq; j += blockDim.x) {
+            const long long i = c0 + s_q[j];
+            const uint32_t pid = A.epid[i];
+            const U4 r = philox4x32_10(U4{pid, (uint32_t)pass, 0u, STREAM_MCC}, A.k0, A.k1);
+            mcc_collide(A, s_tab, i, pid, pass, r, c_el, c_exc, c_ion, c_null, overflow);
+        }
+        __syncthreads();  // the queue is reused by the next chunk
     }
     atomicAdd(&s_cnt[0], (unsigned long long)c_el);
     atomicAdd(&s_cnt[1], (unsigned long long)c_exc);
@@ -332,7 +375,8 @@ pic_status launch_mcc(pic_handle *h)
     A.dev = h->dev;
     mcc_prepare_kernel<<<1, 1, 0, h->stream>>>(h->dev, M.e);
     PIC_CUDA(cudaGetLastError());
-    mcc_kernel<<<grid_for(E.cap, 256), 256, 4 * M.ntab * sizeof(float), h->stream>>>(A);
+    mcc_kernel<<<grid_for(E.cap, MCC_CHUNK), 256,
+                 4 * M.ntab * sizeof(float) + MCC_CHUNK * sizeof(int), h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }
