@@ -1,12 +1,13 @@
-"""Shared setup of the collision tests (not a test module): the BASELINE
-config-3 cross sections and the constants pic_set_mcc derives from them."""
+"""Shared setup of the collision tests (not a test module): the
+electron-neutral cross sections of the 512^2 MCC workload and the
+constants pic_set_mcc derives from them."""
 import numpy as np
 
 E_CH = 1.602176634e-19
 ME = 9.1093837015e-31
 KB = 1.380649e-23
 MI = 73000.0 * ME          # singly charged ion, mass ratio 1/73,000
-M_NEUTRAL = 6.6e-26        # hard-sphere neutral (config 4)
+M_NEUTRAL = 6.6e-26        # hard-sphere neutral of the DSMC workload
 D_NEUTRAL = 3.6e-10
 NG = 3.2e21                # background neutral density, m^-3
 TN_EV = KB * 300.0 / E_CH  # 300 K

@@ -1,6 +1,7 @@
-"""Neutral-neutral DSMC (hard spheres, Bird NTC; BASELINE config 4 gas):
-conservation, relaxation of a bimodal (300 K / 1000 K) gas against the
-oracle's restatement and theory, and the collision rate."""
+"""Neutral-neutral DSMC (hard spheres, Bird NTC; the neutral gas of the
+512^2 MCC + DSMC workload): conservation, relaxation of a bimodal
+(300 K / 1000 K) gas against the oracle's restatement and theory, and the
+collision rate."""
 import numpy as np
 import pytest
 
@@ -86,7 +87,7 @@ def test_dsmc_relaxation_conservation_and_rate():
 
 def test_config4_small_dsmc_with_mcc_electrons():
     """Electrons + ions with MCC and the DSMC neutrals in one step loop
-    (config-4 species on a 64^2 grid, dt = 1e-11 s)."""
+    (the MCC + DSMC workload's species on a 64^2 grid, dt = 1e-11 s)."""
     nx = 64
     L = nx * DX
     ne_ = nx * nx * 16

@@ -1,4 +1,4 @@
-"""Electron-neutral MCC (BASELINE config 3 cross sections, null-collision
+"""Electron-neutral MCC (the 512^2 MCC workload's cross sections, null-collision
 method) against the oracle's restatement on the same Philox streams and
 against the analytic collision frequency."""
 import numpy as np
@@ -107,7 +107,7 @@ def test_mcc_eedf_after_many_passes_matches_oracle():
 
 
 def test_mcc_inside_the_step_config3_small():
-    """Electrons and ions with field and MCC through pic_step (config-3 physics
+    """Electrons and ions with field and MCC through pic_step (the MCC workload's physics
     on a 64^2 grid): charge exact, collisions happen, no device errors."""
     nx, ppc = 64, 16
     n = nx * nx * ppc

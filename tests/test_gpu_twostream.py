@@ -1,4 +1,4 @@
-"""Two-stream instability (BASELINE config 1: 128 x 128 cells, L = 4 pi,
+"""Two-stream instability (the 128 x 128 two-stream run, L = 4 pi,
 100 electrons per cell in two beams +-0.2, dt = 0.1, plasma units)."""
 import numpy as np
 import pytest
@@ -25,7 +25,7 @@ def linear_growth_rate(k, v0, wb2=0.5):
 
 @pytest.mark.parametrize("nx,ny,ppc", [(512, 4, 400), (128, 4, 1600)])
 def test_growth_rate_matches_linear_theory(nx, ny, ppc):
-    """Cold beams +-0.2 in the config-1 domain (Lx = 4 pi, dt = 0.1) on a quiet
+    """Cold beams +-0.2 in the two-stream domain (Lx = 4 pi, dt = 0.1) on a quiet
     (lattice) load, with the growing eigenmode of mode kx = 0.5 loaded:
     |rho^(1,0)| must grow at the cold-beam rate
     gamma = sqrt(-(a^2 + wb^2 - wb sqrt(wb^2 + 4 a^2))), a = k v0, within 2 %.
