@@ -105,6 +105,10 @@ static void free_handle_buffers(pic_handle *h)
     if (h->g_sortstep) cudaGraphExecDestroy(h->g_sortstep);
     if (h->g_one) cudaGraphExecDestroy(h->g_one);
     if (h->cub_temp) cudaFree(h->cub_temp);
+    for (auto &e : h->field_ready)
+        if (e) cudaEventDestroy(e);
+    if (h->copies_done) cudaEventDestroy(h->copies_done);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -707,14 +711,29 @@ pic_status pic_get_particles(pic_handle *h, int s, long long *n, double *x, doub
     if (n) *n = cnt;
     const size_t nn = (size_t)cnt;
     if (!nn) return PIC_OK;
-    PIC_TRY(ensure_stage(h, nn * 5 * sizeof(double)));
+    // id order through the inverse of the id permutation (coalesced writes),
+    // each field copied to the host on the copy stream while the next one
+    // is gathered
+    const size_t cap = (size_t)h->sp[s].cap;
+    PIC_TRY(ensure_stage(h, nn * 5 * sizeof(double) + cap * sizeof(uint32_t)));
     double *d = (double *)h->stage;
-    PIC_TRY(launch_to_global(h, s, d, d + nn, d + 2 * nn, d + 3 * nn, vz ? d + 4 * nn : nullptr));
-    if (x) PIC_CUDA(cudaMemcpyAsync(x, d, nn * 8, cudaMemcpyDeviceToHost, h->stream));
-    if (y) PIC_CUDA(cudaMemcpyAsync(y, d + nn, nn * 8, cudaMemcpyDeviceToHost, h->stream));
-    if (vx) PIC_CUDA(cudaMemcpyAsync(vx, d + 2 * nn, nn * 8, cudaMemcpyDeviceToHost, h->stream));
-    if (vy) PIC_CUDA(cudaMemcpyAsync(vy, d + 3 * nn, nn * 8, cudaMemcpyDeviceToHost, h->stream));
-    if (vz) PIC_CUDA(cudaMemcpyAsync(vz, d + 4 * nn, nn * 8, cudaMemcpyDeviceToHost, h->stream));
+    uint32_t *inv = (uint32_t *)(d + 5 * nn);
+    if (!h->copy_stream) {
+        PIC_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (auto &e : h->field_ready) PIC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        PIC_CUDA(cudaEventCreateWithFlags(&h->copies_done, cudaEventDisableTiming));
+    }
+    double *host[5] = {x, y, vx, vy, vz};
+    double *dev[5];
+    for (int k = 0; k < 5; ++k) dev[k] = host[k] ? d + k * nn : nullptr;
+    PIC_TRY(launch_to_global_by_id(h, s, dev, inv, h->field_ready));
+    for (int k = 0; k < 5; ++k) {
+        if (!host[k]) continue;
+        PIC_CUDA(cudaStreamWaitEvent(h->copy_stream, h->field_ready[k], 0));
+        PIC_CUDA(cudaMemcpyAsync(host[k], dev[k], nn * 8, cudaMemcpyDeviceToHost, h->copy_stream));
+    }
+    PIC_CUDA(cudaEventRecord(h->copies_done, h->copy_stream));
+    PIC_CUDA(cudaStreamWaitEvent(h->stream, h->copies_done, 0));
     PIC_CUDA(cudaStreamSynchronize(h->stream));
     return PIC_OK;
 }

@@ -144,6 +144,38 @@ __global__ void to_global_kernel(const int32_t *cell, const float *ox, const flo
     }
 }
 
+// inv[pid[i]] = i for the n live slots (ids are a permutation of 0..n-1)
+__global__ void id_inverse_kernel(const uint32_t *__restrict__ pid, const long long *d_n,
+                                  uint32_t *__restrict__ inv)
+{
+    const long long n = *d_n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t p = pid[i];
+        if ((long long)p < n) inv[p] = (uint32_t)i;
+    }
+}
+
+// One exported field in id order: out[p] from slot inv[p] (coalesced writes,
+// gathered reads).  field: 0 x, 1 y, 2 vx, 3 vy, 4 vz.
+__global__ void id_gather_kernel(const uint32_t *__restrict__ inv, const long long *d_n, int field,
+                                 const int32_t *__restrict__ cell, const float *__restrict__ off,
+                                 const float *__restrict__ v, double d, double *__restrict__ out)
+{
+    const long long n = *d_n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+        const uint32_t i = inv[p];
+        if ((long long)i >= n) continue;  // an id no slot carries
+        if (field == 0)
+            out[p] = ((double)(cell[i] & 0xFFFF) + (double)off[i]) * d;
+        else if (field == 1)
+            out[p] = ((double)(cell[i] >> 16) + (double)off[i]) * d;
+        else
+            out[p] = v ? (double)v[i] : 0.0;
+    }
+}
+
 __global__ void fill_padding_kernel(int32_t *c0, int32_t *c1, long long from, long long to)
 {
     const long long i = from + (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -315,15 +347,30 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
     return PIC_OK;
 }
 
-pic_status launch_to_global(pic_handle *h, int s, double *x_dev, double *y_dev, double *vx_dev,
-                            double *vy_dev, double *vz_dev)
+// Export of species s in id order into five device arrays out[0..4] (x, y,
+// vx, vy, vz; null entries skipped) through the slot-of-id inverse (`inv`,
+// cap words); after each field's gather `ready[k]` is recorded on the
+// handle's stream, so that a copy of field k can start while the next
+// field is gathered.
+pic_status launch_to_global_by_id(pic_handle *h, int s, double *const *out, uint32_t *inv,
+                                  cudaEvent_t *ready)
 {
     SpeciesBuf &B = h->sp[s];
     if (B.cap == 0) return PIC_OK;
-    to_global_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(
-        B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.vz[0], B.pid[0], &h->dev->n[s], h->g.dx,
-        h->g.dy, x_dev, y_dev, vx_dev, vy_dev, vz_dev);
+    const long long *d_n = &h->dev->n[s];
+    PIC_CUDA(cudaMemsetAsync(inv, 0xFF, sizeof(uint32_t) * (size_t)B.cap, h->stream));
+    id_inverse_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(B.pid[0], d_n, inv);
     PIC_CUDA(cudaGetLastError());
+    const float *off[5] = {B.ox[0], B.oy[0], nullptr, nullptr, nullptr};
+    const float *vel[5] = {nullptr, nullptr, B.vx[0], B.vy[0], B.vz[0]};
+    const double dd[5] = {h->g.dx, h->g.dy, 0.0, 0.0, 0.0};
+    for (int k = 0; k < 5; ++k) {
+        if (!out[k]) continue;
+        id_gather_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(inv, d_n, k, B.cell[0], off[k],
+                                                                       vel[k], dd[k], out[k]);
+        PIC_CUDA(cudaGetLastError());
+        PIC_CUDA(cudaEventRecord(ready[k], h->stream));
+    }
     return PIC_OK;
 }
 

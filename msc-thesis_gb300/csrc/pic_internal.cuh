@@ -183,6 +183,10 @@ struct pic_handle {
     // radix sort temporary storage of the import sort
     void *cub_temp = nullptr;
     size_t cub_temp_bytes = 0;
+    // export: copies to the host on their own stream, field by field
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t field_ready[5] = {};
+    cudaEvent_t copies_done = nullptr;
 };
 
 namespace pic {
@@ -216,8 +220,8 @@ pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_
 pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x_dev,
                               const double *y_dev, const double *vx_dev, const double *vy_dev,
                               const double *vz_dev);
-pic_status launch_to_global(pic_handle *h, int s, double *x_dev, double *y_dev, double *vx_dev,
-                            double *vy_dev, double *vz_dev);
+pic_status launch_to_global_by_id(pic_handle *h, int s, double *const *out, uint32_t *inv,
+                                  cudaEvent_t *ready);
 pic_status launch_fill_padding(pic_handle *h, int s, long long from, long long to);
 pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
                           double *dxdA, double *dydA);
