@@ -136,3 +136,31 @@ def test_autotune_picks_a_working_config():
         h.init_particles(0, spec)
         h.step(5)
         assert h.diagnostics().error_flags == 0
+
+
+@pytest.mark.parametrize("nx,ny", [(45, 27), (33, 64)])
+def test_odd_grids_match_fp64_oracle(nx, ny):
+    """Odd cell counts: no Nyquist column or row, odd node count for the
+    density conversion, tiles that do not divide by powers of two."""
+    Lx, Ly = nx * 0.11, ny * 0.07
+    n = nx * ny * 12
+    cfg, q, m = normalized_electrons(nx, ny, Lx, Ly, n, 0.05, sort_every=3)
+    with P.Handle(cfg) as h:
+        h.init_particles(0, P.init_spec(n, vth=(0.3, 0.2, 0), pert_kind=P.PERT_DENSITY,
+                                        pert_amp=0.05, pert_mx=1, pert_my=2, seed=8))
+        st = oracle_from_handle(h, cfg, q, m)
+        h.prime_leapfrog()
+        st.prime(nthreads=0)
+        nst = 20
+        h.step(nst)
+        ref = st.run(nst, nthreads=0)
+        fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
+        d = h.diagnostics()
+        a = h.get_particles()
+    rel = np.abs(fe - ref["fe"]) / ref["fe"].max()
+    print(nx, ny, "field energy max rel err", rel.max())
+    assert rel.max() < 2e-4
+    assert d.total_charge_fixed == d.expected_charge_fixed
+    s = st.species[0]
+    assert np.abs(periodic_diff(a["x"], s["x"], Lx)).max() < 1e-3 * Lx / nx
+    assert np.abs(periodic_diff(a["y"], s["y"], Ly)).max() < 1e-3 * Ly / ny
