@@ -103,14 +103,41 @@ __device__ __forceinline__ void red_cell(float *gx, float *gy, int c, int nx, in
     atomicAdd(gy + w.i11, v[7]);
 }
 
+// the same eight sums into the block's window (shared-memory float adds)
+// when the cell lies in it, else straight to the grid
+__device__ __forceinline__ void red_cell_win(const Window &W, int wcx, int wcy, float *gx, float *gy,
+                                             int c, int nx, int ny, const float (&v)[8])
+{
+    int dxl = (c & 0xFFFF) - W.wx0, dyl = (c >> 16) - W.wy0;
+    if (dxl < 0) dxl += nx;
+    if (dyl < 0) dyl += ny;
+    if (W.on && dxl < wcx && dyl < wcy) {
+        float *sx = reinterpret_cast<float *>(W.sLo), *sy = reinterpret_cast<float *>(W.sHi);
+        const int l = dyl * W.nwx + dxl;
+        atomicAdd(sx + l, v[0]);
+        atomicAdd(sy + l, v[1]);
+        atomicAdd(sx + l + 1, v[2]);
+        atomicAdd(sy + l + 1, v[3]);
+        atomicAdd(sx + l + W.nwx, v[4]);
+        atomicAdd(sy + l + W.nwx, v[5]);
+        atomicAdd(sx + l + W.nwx + 1, v[6]);
+        atomicAdd(sy + l + W.nwx + 1, v[7]);
+    } else {
+        red_cell(gx, gy, c, nx, ny, v);
+    }
+}
+
 // Drift adjoint, kick transpose (scatter of mu and local term) and, with
 // UNKICK, the reversal of the kick.  One push block of particles per CTA;
 // each lane owns four consecutive particles (128-bit loads), E comes from
 // the block's shared-memory window (global loads outside it).  Scatter
 // contributions are summed in registers over a lane's particles in one
-// cell, then over the warp's lanes in one cell (warp_run_sum8), and added
-// to the global planes by the run's first lane (shared-memory float
-// atomics measured slower than these global reductions).
+// cell, then over the warp's lanes in one cell (warp_run_sum8); the run's
+// first lane adds them to the block's window (the deposit window's two
+// planes, here as float x and y sums), which is flushed to the grid at the
+// end.  Cells outside the window go to the grid directly.  Window adds
+// without the warp sums measured 8% slower, global reductions without
+// the window 4% slower.
 template <bool UNKICK>
 __global__ void __launch_bounds__(256, 3)
 ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs,
@@ -122,6 +149,8 @@ ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun
     const PushGeo G = adj_geo(R, A.e);
     const Window W = setup_window(G, smem, anchor[blockIdx.x]);
     load_window<true, false>(G, W);
+    if (W.on)
+        for (int i = threadIdx.x; i < W.nw; i += blockDim.x) W.sLo[i] = W.sHi[i] = 0u;
     __syncthreads();
     float *ggx = A.g + 2 * R.goff, *ggy = ggx + R.ncp;
     const float qmdt = R.qm_dt, muc = cscale * R.qm_dt, ddt = dscale * R.dt;
@@ -190,7 +219,7 @@ ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun
 #pragma unroll
                 for (int k = 0; k < 8; ++k) acc[k] += v[k];
             } else {
-                red_cell(ggx, ggy, c, nx, ny, v);
+                red_cell_win(W, G.wcx, G.wcy, ggx, ggy, c, nx, ny, v);
             }
             const float s00 = e00.x * mx + e00.y * my, s10 = e10.x * mx + e10.y * my;
             const float s01 = e01.x * mx + e01.y * my, s11 = e11.x * mx + e11.y * my;
@@ -205,7 +234,7 @@ ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun
                 vy[j] = fmaf(-qmdt, Ey, vy[j]);
             }
         }
-        if (warp_run_sum8(gkey, acc) && gkey >= 0) red_cell(ggx, ggy, gkey, nx, ny, acc);
+        if (warp_run_sum8(gkey, acc) && gkey >= 0) red_cell_win(W, G.wcx, G.wcy, ggx, ggy, gkey, nx, ny, acc);
         if (live) {
             *reinterpret_cast<float4 *>(A.ax + q) = make_float4(ax[0], ax[1], ax[2], ax[3]);
             *reinterpret_cast<float4 *>(A.ay + q) = make_float4(ay[0], ay[1], ay[2], ay[3]);
@@ -216,6 +245,17 @@ ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun
                 *reinterpret_cast<float4 *>(A.vy + q) = make_float4(vy[0], vy[1], vy[2], vy[3]);
             }
         }
+    }
+    if (!W.on) return;
+    __syncthreads();
+    const float *sx = reinterpret_cast<const float *>(W.sLo), *sy = reinterpret_cast<const float *>(W.sHi);
+    for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
+        const float fx = sx[i], fy = sy[i];
+        if (fx == 0.f && fy == 0.f) continue;
+        const int gxn = (W.wx0 + i % W.nwx) % nx, gyn = (W.wy0 + i / W.nwx) % ny;
+        const size_t o = (size_t)gyn * nx + gxn;
+        if (fx != 0.f) atomicAdd(ggx + o, fx);
+        if (fy != 0.f) atomicAdd(ggy + o, fy);
     }
 }
 
