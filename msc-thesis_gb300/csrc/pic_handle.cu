@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -292,8 +293,9 @@ static pic_status sort_now(pic_handle *h, bool import = false)
 {
     for (int s = 0; s < h->cfg.nspecies; ++s) {
         if (!h->sp[s].cap) continue;
-        PIC_TRY(import ? import_sort(h, s) : launch_sort(h, s));
-        PIC_TRY(copy_back(h, s));
+        bool in0 = false;
+        PIC_TRY(import ? import_sort(h, s, &in0) : launch_sort(h, s));
+        if (!in0) PIC_TRY(copy_back(h, s));
     }
     h->since_sort = 0;
     return PIC_OK;
@@ -397,6 +399,26 @@ template <class T> static T *mapped(T *p)
         return nullptr;
     }
     return a.type == cudaMemoryTypeHost ? (T *)a.devicePointer : nullptr;
+}
+
+// Whether the stage holds `bytes` now or can grow to it and leave 1 GiB of
+// device memory free (callers fall back to a leaner layout otherwise).  The
+// environment variable PIC_STAGE_MAX_BYTES caps the layouts chosen this way
+// for callers that keep a device-memory budget.
+bool stage_fits(pic_handle *h, size_t bytes)
+{
+    if (const char *cap = getenv("PIC_STAGE_MAX_BYTES")) {
+        char *end = nullptr;
+        const unsigned long long v = strtoull(cap, &end, 10);
+        if (end != cap && bytes > v) return false;
+    }
+    if (h->stage_bytes >= bytes) return true;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return free_b + h->stage_bytes >= bytes + (1ull << 30);
 }
 
 pic_status ensure_stage(pic_handle *h, size_t bytes)
@@ -711,12 +733,19 @@ pic_status pic_get_particles(pic_handle *h, int s, long long *n, double *x, doub
     if (n) *n = cnt;
     const size_t nn = (size_t)cnt;
     if (!nn) return PIC_OK;
-    // id order through the inverse of the id permutation (coalesced writes),
-    // each field copied to the host on the copy stream while the next one
-    // is gathered
+    // id order: the slots' fields scattered as one 32-byte record per id
+    // (or, when the stage cannot hold the records, through the inverse of
+    // the id permutation), then each field converted with coalesced writes
+    // and copied to the host on the copy stream while the next one is
+    // converted
     const size_t cap = (size_t)h->sp[s].cap;
-    PIC_TRY(ensure_stage(h, nn * 5 * sizeof(double) + cap * sizeof(uint32_t)));
-    double *d = (double *)h->stage;
+    const size_t packed_bytes = nn * (32 + 5 * sizeof(double));
+    const bool packed = stage_fits(h, packed_bytes);
+    PIC_TRY(ensure_stage(h, packed ? packed_bytes : nn * 5 * sizeof(double) + cap * sizeof(uint32_t)));
+    // packed: records (16-byte aligned) then the doubles; else the doubles
+    // then the inverse permutation
+    uint4 *rec = (uint4 *)h->stage;
+    double *d = packed ? (double *)(rec + 2 * nn) : (double *)h->stage;
     uint32_t *inv = (uint32_t *)(d + 5 * nn);
     if (!h->copy_stream) {
         PIC_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
@@ -726,7 +755,10 @@ pic_status pic_get_particles(pic_handle *h, int s, long long *n, double *x, doub
     double *host[5] = {x, y, vx, vy, vz};
     double *dev[5];
     for (int k = 0; k < 5; ++k) dev[k] = host[k] ? d + k * nn : nullptr;
-    PIC_TRY(launch_to_global_by_id(h, s, dev, inv, h->field_ready));
+    if (packed)
+        PIC_TRY(launch_to_global_by_record(h, s, dev, rec, h->field_ready));
+    else
+        PIC_TRY(launch_to_global_by_id(h, s, dev, inv, h->field_ready));
     for (int k = 0; k < 5; ++k) {
         if (!host[k]) continue;
         PIC_CUDA(cudaStreamWaitEvent(h->copy_stream, h->field_ready[k], 0));

@@ -64,6 +64,42 @@ __global__ void import_gather_kernel(Fields F, const uint32_t *__restrict__ src,
     }
 }
 
+// Keys and slots as above, and every field of the slot packed into one
+// 32-byte record {cell, ox, oy, vx}, {vy, pid, vz, 0}: after the sort the
+// permuted read of a particle touches one DRAM sector instead of one per
+// field (vz may be absent).
+__global__ void import_pack_kernel(Fields F, long long n, KeyGeo G, unsigned *err,
+                                   uint32_t *__restrict__ keys, uint32_t *__restrict__ idx,
+                                   uint4 *__restrict__ rec)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t c = F.in[0][i];
+        keys[i] = (uint32_t)particle_key(G, err, (int)c);
+        idx[i] = (uint32_t)i;
+        rec[2 * i] = make_uint4(c, F.in[1][i], F.in[2][i], F.in[3][i]);
+        rec[2 * i + 1] = make_uint4(F.in[4][i], F.in[5][i], F.nf > 6 ? F.in[6][i] : 0u, 0u);
+    }
+}
+
+// out_f[i] = field f of record src[i]
+__global__ void import_unpack_kernel(Fields F, const uint4 *__restrict__ rec,
+                                     const uint32_t *__restrict__ src, long long n)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const size_t j = src[i];
+        const uint4 a = rec[2 * j], b = rec[2 * j + 1];
+        F.out[0][i] = a.x;
+        F.out[1][i] = a.y;
+        F.out[2][i] = a.z;
+        F.out[3][i] = a.w;
+        F.out[4][i] = b.x;
+        F.out[5][i] = b.y;
+        if (F.nf > 6) F.out[6][i] = b.z;
+    }
+}
+
 namespace {
 
 int key_bits(long long nkeys)
@@ -96,10 +132,14 @@ pic_status radix_pairs(uint32_t *scratch, long long n, int bits, void **temp, si
 
 }  // namespace
 
-// Species s of a handle, live in buffer 0 in arbitrary order -> buffer 1 in
-// key order (the caller copies back), anchors from buffer 1.
-pic_status import_sort(pic_handle *h, int s)
+// Species s of a handle, live in buffer 0 in arbitrary order -> key order,
+// with the chunk anchors.  The fields travel as packed records when the
+// stage can hold them (48 bytes per slot) and land back in buffer 0
+// (*in_buffer0 = true); else each field is gathered on its own into buffer 1
+// (16 bytes per slot) and the caller copies back.
+pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
 {
+    *in_buffer0 = false;
     SpeciesBuf &B = h->sp[s];
     const long long n = B.cap;  // padding slots (cell -1) sort to the end
     if (!n) return PIC_OK;
@@ -108,27 +148,38 @@ pic_status import_sort(pic_handle *h, int s)
         return PIC_ERR_INVALID_ARG;
     }
     const Geometry &g = h->g;
-    PIC_TRY(ensure_stage(h, (size_t)n * 16));
+    const bool packed = stage_fits(h, (size_t)n * 48);
+    PIC_TRY(ensure_stage(h, (size_t)n * (packed ? 48 : 16)));
     uint32_t *scratch = (uint32_t *)h->stage;
+    uint4 *rec = reinterpret_cast<uint4 *>(scratch + 4 * n);
     const KeyGeo G{g.nx, g.ny, g.tw, g.th, g.ntx, 0};
-    import_keys_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(B.cell[0], n, G, &h->dev->err,
-                                                                scratch, scratch + 2 * n);
-    PIC_CUDA(cudaGetLastError());
-    const uint32_t *idx = nullptr;
-    PIC_TRY(radix_pairs(scratch, n, key_bits((long long)g.nx * g.ny + 1), &h->cub_temp,
-                        &h->cub_temp_bytes, h->stream, &idx));
     Fields F;
     memset(&F, 0, sizeof F);
     const void *in[7] = {B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.pid[0], B.vz[0]};
-    void *out[7] = {B.cell[1], B.ox[1], B.oy[1], B.vx[1], B.vy[1], B.pid[1], B.vz[1]};
+    const int ob = packed ? 0 : 1;
+    void *out[7] = {B.cell[ob], B.ox[ob], B.oy[ob], B.vx[ob], B.vy[ob], B.pid[ob], B.vz[ob]};
     F.nf = B.vz[0] ? 7 : 6;
     for (int f = 0; f < F.nf; ++f) {
         F.in[f] = (const uint32_t *)in[f];
         F.out[f] = (uint32_t *)out[f];
     }
-    import_gather_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(F, idx, n);
+    if (packed)
+        import_pack_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(F, n, G, &h->dev->err, scratch,
+                                                                    scratch + 2 * n, rec);
+    else
+        import_keys_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(B.cell[0], n, G, &h->dev->err,
+                                                                    scratch, scratch + 2 * n);
     PIC_CUDA(cudaGetLastError());
-    return launch_anchors(h, s);
+    const uint32_t *idx = nullptr;
+    PIC_TRY(radix_pairs(scratch, n, key_bits((long long)g.nx * g.ny + 1), &h->cub_temp,
+                        &h->cub_temp_bytes, h->stream, &idx));
+    if (packed)
+        import_unpack_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(F, rec, idx, n);
+    else
+        import_gather_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(F, idx, n);
+    PIC_CUDA(cudaGetLastError());
+    *in_buffer0 = packed;
+    return launch_anchors(h, s, ob);
 }
 
 // Every run of an ensemble: buffer 0 in arbitrary order -> buffer 1 in key

@@ -176,6 +176,53 @@ __global__ void id_gather_kernel(const uint32_t *__restrict__ inv, const long lo
     }
 }
 
+// Export through packed records: every slot's fields scattered to the
+// record of its id, {cell, ox, oy, vx}, {vy, vz, cell, 0}, one 32-byte
+// sector per particle written whole.  Records of ids no slot carries keep
+// the 0xFF fill (cell -1).
+__global__ void id_record_kernel(const int32_t *__restrict__ cell, const float *__restrict__ ox,
+                                 const float *__restrict__ oy, const float *__restrict__ vx,
+                                 const float *__restrict__ vy, const float *__restrict__ vz,
+                                 const uint32_t *__restrict__ pid, const long long *d_n,
+                                 uint4 *__restrict__ rec)
+{
+    const long long n = *d_n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const size_t p = pid[i];
+        if ((long long)p >= n) continue;
+        const uint32_t c = (uint32_t)cell[i];
+        rec[2 * p] = make_uint4(c, __float_as_uint(ox[i]), __float_as_uint(oy[i]), __float_as_uint(vx[i]));
+        rec[2 * p + 1] = make_uint4(__float_as_uint(vy[i]), vz ? __float_as_uint(vz[i]) : 0u, c, 0u);
+    }
+}
+
+// One exported field in id order from the records (coalesced both ways).
+// field: 0 x, 1 y, 2 vx, 3 vy, 4 vz.
+__global__ void id_record_field_kernel(const uint4 *__restrict__ rec, const long long *d_n, int field,
+                                       double d, double *__restrict__ out)
+{
+    const long long n = *d_n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+        if (field <= 2) {
+            const uint4 a = rec[2 * p];
+            const int c = (int)a.x;
+            if (c < 0) continue;  // an id no slot carries
+            if (field == 0)
+                out[p] = ((double)(c & 0xFFFF) + (double)__uint_as_float(a.y)) * d;
+            else if (field == 1)
+                out[p] = ((double)(c >> 16) + (double)__uint_as_float(a.z)) * d;
+            else
+                out[p] = (double)__uint_as_float(a.w);
+        } else {
+            const uint4 b = rec[2 * p + 1];
+            if ((int)b.z < 0) continue;
+            out[p] = (double)__uint_as_float(field == 3 ? b.x : b.y);
+        }
+    }
+}
+
 __global__ void fill_padding_kernel(int32_t *c0, int32_t *c1, long long from, long long to)
 {
     const long long i = from + (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -368,6 +415,26 @@ pic_status launch_to_global_by_id(pic_handle *h, int s, double *const *out, uint
         if (!out[k]) continue;
         id_gather_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(inv, d_n, k, B.cell[0], off[k],
                                                                        vel[k], dd[k], out[k]);
+        PIC_CUDA(cudaGetLastError());
+        PIC_CUDA(cudaEventRecord(ready[k], h->stream));
+    }
+    return PIC_OK;
+}
+
+pic_status launch_to_global_by_record(pic_handle *h, int s, double *const *out, uint4 *rec,
+                                      cudaEvent_t *ready)
+{
+    SpeciesBuf &B = h->sp[s];
+    if (B.cap == 0) return PIC_OK;
+    const long long *d_n = &h->dev->n[s];
+    PIC_CUDA(cudaMemsetAsync(rec, 0xFF, 32 * (size_t)B.n, h->stream));
+    id_record_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(
+        B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.vz[0], B.pid[0], d_n, rec);
+    PIC_CUDA(cudaGetLastError());
+    const double dd[5] = {h->g.dx, h->g.dy, 0.0, 0.0, 0.0};
+    for (int k = 0; k < 5; ++k) {
+        if (!out[k]) continue;
+        id_record_field_kernel<<<grid_for(B.n, 256), 256, 0, h->stream>>>(rec, d_n, k, dd[k], out[k]);
         PIC_CUDA(cudaGetLastError());
         PIC_CUDA(cudaEventRecord(ready[k], h->stream));
     }

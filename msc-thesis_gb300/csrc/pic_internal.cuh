@@ -204,9 +204,10 @@ pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s);
 pic_status scatter_smem_attr(const void *kernel);
-pic_status launch_anchors(pic_handle *h, int s);
-// pic_import.cu: arbitrary order in buffer 0 -> key order in buffer 1 (+ anchors)
-pic_status import_sort(pic_handle *h, int s);
+pic_status launch_anchors(pic_handle *h, int s, int buf = 1);
+// pic_import.cu: arbitrary order in buffer 0 -> key order in buffer 0 (records)
+// or buffer 1 (per-field gather), with the anchors
+pic_status import_sort(pic_handle *h, int s, bool *in_buffer0);
 // exclusive scan of count[0, nkeys) into offset and cursor, offset[nkeys] =
 // *d_total; bsum, bsum_s: ceil(nkeys / 4096) entries, bsum2: ceil(that / 4096)
 pic_status launch_key_scan(const uint32_t *count, uint32_t *offset, uint32_t *cursor,
@@ -222,6 +223,8 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
                               const double *vz_dev);
 pic_status launch_to_global_by_id(pic_handle *h, int s, double *const *out, uint32_t *inv,
                                   cudaEvent_t *ready);
+pic_status launch_to_global_by_record(pic_handle *h, int s, double *const *out, uint4 *rec,
+                                      cudaEvent_t *ready);
 pic_status launch_fill_padding(pic_handle *h, int s, long long from, long long to);
 pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
                           double *dxdA, double *dydA);
@@ -251,6 +254,7 @@ pic_status record_push_all(pic_handle *h, int src, bool deposit);
 pic_status deposit_now(pic_handle *h);
 pic_status refresh(pic_handle *h);
 pic_status ensure_stage(pic_handle *h, size_t bytes);
+bool stage_fits(pic_handle *h, size_t bytes);
 pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly);
 pic_status lattice_dims_for(int nx, int ny, long long n, int *lx, int *ly);
 int pick_divisor(int n, int target);

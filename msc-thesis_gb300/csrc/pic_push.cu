@@ -36,7 +36,9 @@
 namespace pic {
 
 // Direct-load variant: each thread loads its quads with 128-bit loads.
-template <bool GATHER, bool DEPOSIT, bool AGG>
+// !MOVE: the deposit of the particles where they are (after an import, a
+// sort or a state load), through the same shared-memory windows.
+template <bool GATHER, bool DEPOSIT, bool AGG, bool MOVE = true>
 __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -44,8 +46,8 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs A)
     const long long base = (long long)blockIdx.x * A.chunk;
     if (base >= n) return;  // block-uniform
     const long long n4 = (n + 3) & ~3ll;
-    push_block<GATHER, DEPOSIT, AGG>(A, A.geo, smem, base, min(base + (long long)A.chunk, n4),
-                                     A.anchor[blockIdx.x]);
+    push_block<GATHER, DEPOSIT, AGG, MOVE>(A, A.geo, smem, base, min(base + (long long)A.chunk, n4),
+                                           A.anchor[blockIdx.x]);
 }
 
 // ------------------------------------------------------------------------
@@ -254,12 +256,11 @@ template <bool G, bool D> static pic_status bulk_attr(size_t sm)
     return PIC_OK;
 }
 
-pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale)
+static PushArgs push_args(pic_handle *h, int s, int src, float dt_scale)
 {
     SpeciesBuf &B = h->sp[s];
     const pic_species_desc &D = h->cfg.species[s];
     const Geometry &g = h->g;
-    if (B.nchunks == 0) return PIC_OK;
     PushArgs A;
     A.cin = B.cell[src];
     A.oxin = B.ox[src];
@@ -298,6 +299,16 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
     A.geo.qmul = (unsigned long long)(long long)D.q_int;
     A.geo.ke_scale = move ? 0.25 * D.m : 0.0;
     A.geo.p_scale = 0.5 * D.m;
+    return A;
+}
+
+pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale)
+{
+    SpeciesBuf &B = h->sp[s];
+    const pic_species_desc &D = h->cfg.species[s];
+    const Geometry &g = h->g;
+    if (B.nchunks == 0) return PIC_OK;
+    PushArgs A = push_args(h, s, src, dt_scale);
     const bool charged = D.q != 0.0;
     const bool dep = deposit && D.q_int != 0;
     dim3 grid((unsigned)B.nchunks), block(256);
@@ -343,14 +354,16 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
     return PIC_OK;
 }
 
+// Deposit of buffer 0 where it stands: shared-memory windows at the chunk
+// anchors (particles outside a stale window go straight to the grid), the
+// particle arrays only read.
 pic_status launch_deposit(pic_handle *h, int s)
 {
     SpeciesBuf &B = h->sp[s];
     const pic_species_desc &D = h->cfg.species[s];
-    if (D.q_int == 0 || B.cap == 0) return PIC_OK;
-    deposit_flat_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(
-        B.cell[0], B.ox[0], B.oy[0], &h->dev->n[s], 0, h->g.nx, h->g.ny,
-        (unsigned long long)(long long)D.q_int, h->rho_fix, &h->dev->err);
+    if (D.q_int == 0 || B.cap == 0 || B.nchunks == 0) return PIC_OK;
+    const PushArgs A = push_args(h, s, 0, 0.f);
+    push_kernel<false, true, false, false><<<(unsigned)B.nchunks, 256, push_smem(h->g), h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }

@@ -170,8 +170,9 @@ __device__ __forceinline__ bool warp_group_sum(int key, unsigned &c, unsigned &f
 // AGG: the lanes' main groups are summed across the warp (warp_group_sum)
 // before the deposit, so that a warp whose particles share a cell issues
 // one set of atomics instead of 32 conflicting ones; every lane of the warp
-// must then call this function together.
-template <bool GATHER, bool DEPOSIT, bool AGG>
+// must then call this function together.  !MOVE: deposit the particles
+// where they are (no gather, no push, velocities not read).
+template <bool GATHER, bool DEPOSIT, bool AGG, bool MOVE = true>
 __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int (&cc)[4],
                                           float (&xo)[4], float (&yo)[4], float (&xv)[4],
                                           float (&yv)[4], float &ke, float &px, float &py,
@@ -193,7 +194,8 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
             continue;
         }
         float ox = xo[j], oy = yo[j], vx = xv[j], vy = yv[j];
-        if (GATHER) {
+        if (!MOVE) {
+        } else if (GATHER) {
             const float gx = 1.f - ox, gy = 1.f - oy;
             float2 e00, e10, e01, e11;
             int dxl = cx - W.wx0, dyl = cy - W.wy0;
@@ -228,19 +230,21 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
             px = fmaf(2.f, vx, px);
             py = fmaf(2.f, vy, py);
         }
-        bad |= !(fabsf(vx) <= 3.0e38f) || !(fabsf(vy) <= 3.0e38f);
-        // drift in cell units; carry whole cells into the index
-        ox = fmaf(vx, A.dtdx, ox);
-        oy = fmaf(vy, A.dtdy, oy);
-        float sx = floorf(ox), sy = floorf(oy);
-        ox -= sx;
-        oy -= sy;
-        if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
-        if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
-        cx += (int)sx;
-        cy += (int)sy;
-        if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
-        if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
+        if (MOVE) {
+            bad |= !(fabsf(vx) <= 3.0e38f) || !(fabsf(vy) <= 3.0e38f);
+            // drift in cell units; carry whole cells into the index
+            ox = fmaf(vx, A.dtdx, ox);
+            oy = fmaf(vy, A.dtdy, oy);
+            float sx = floorf(ox), sy = floorf(oy);
+            ox -= sx;
+            oy -= sy;
+            if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
+            if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
+            cx += (int)sx;
+            cy += (int)sy;
+            if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
+            if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
+        }
         const int cn = cx | (cy << 16);
         cc[j] = cn;
         xo[j] = ox;
@@ -334,7 +338,8 @@ __device__ __forceinline__ void finish_block(const PushGeo &A, const Window &W, 
 // the end of the padded array), window anchored at tile `anc` (-1: none).
 // Thread t owns the quads base + 4t + 4k blockDim.x; the loop runs while any
 // lane of the warp has a quad, so that the warp stays converged for AGG.
-template <bool GATHER, bool DEPOSIT, bool AGG>
+// !MOVE: a deposit of the particles in place; nothing is stored.
+template <bool GATHER, bool DEPOSIT, bool AGG, bool MOVE = true>
 __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, unsigned char *smem,
                                            long long base, long long end, int anc)
 {
@@ -360,19 +365,21 @@ __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, 
                 const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);
                 const float4 a4 = *reinterpret_cast<const float4 *>(A.oxin + q);
                 const float4 b4 = *reinterpret_cast<const float4 *>(A.oyin + q);
-                const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
-                const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
                 cc[0] = c4.x, cc[1] = c4.y, cc[2] = c4.z, cc[3] = c4.w;
                 xo[0] = a4.x, xo[1] = a4.y, xo[2] = a4.z, xo[3] = a4.w;
                 yo[0] = b4.x, yo[1] = b4.y, yo[2] = b4.z, yo[3] = b4.w;
-                xv[0] = u4.x, xv[1] = u4.y, xv[2] = u4.z, xv[3] = u4.w;
-                yv[0] = v4.x, yv[1] = v4.y, yv[2] = v4.z, yv[3] = v4.w;
+                if (MOVE) {
+                    const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+                    const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+                    xv[0] = u4.x, xv[1] = u4.y, xv[2] = u4.z, xv[3] = u4.w;
+                    yv[0] = v4.x, yv[1] = v4.y, yv[2] = v4.z, yv[3] = v4.w;
+                }
             }
-            push_quad<GATHER, DEPOSIT, AGG>(G, W, cc, xo, yo, xv, yv, ke, px, py, bad);
-            if (live) store_quad(A, q, cc, xo, yo, xv, yv);
+            push_quad<GATHER, DEPOSIT, AGG, MOVE>(G, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+            if (MOVE && live) store_quad(A, q, cc, xo, yo, xv, yv);
         }
     }
-    finish_block<DEPOSIT>(G, W, sAcc, ke, px, py, bad);
+    finish_block<DEPOSIT>(G, W, sAcc, ke, px, py, MOVE && bad);
 }
 
 }  // namespace pic

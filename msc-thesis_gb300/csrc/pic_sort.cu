@@ -196,15 +196,15 @@ pic_status scatter_smem_attr(const void *kernel)
     return PIC_OK;
 }
 
-// Chunk anchors of species s from the sorted order in buffer 1.
-pic_status launch_anchors(pic_handle *h, int s)
+// Chunk anchors of species s from the sorted order in buffer `buf`.
+pic_status launch_anchors(pic_handle *h, int s, int buf)
 {
     SpeciesBuf &B = h->sp[s];
     const Geometry &g = h->g;
     if (!B.nchunks) return PIC_OK;
     SortArgs A;
     memset(&A, 0, sizeof A);
-    A.cout = B.cell[1];
+    A.cout = B.cell[buf];
     A.anchor = B.anchor;
     A.d_n = &h->dev->n[s];
     A.nx = g.nx;

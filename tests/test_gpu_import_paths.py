@@ -1,0 +1,76 @@
+"""Imports and exports through packed 32-byte particle records against the
+per-field gathers used when the stage may not grow (PIC_STAGE_MAX_BYTES):
+identical sorted state, identical runs, identical exports, from page-locked
+and from pageable host arrays, with and without a third velocity."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import picgpu as P
+from gpu_util import normalized_electrons
+
+pytestmark = pytest.mark.gpu
+
+NX, NY = 64, 48
+
+
+def _particles(n, seed, vz=False):
+    rng = np.random.default_rng(seed)
+    x = rng.random(n) * 8.0
+    y = rng.random(n) * 6.0
+    v = [rng.normal(0.0, 0.3, n) for _ in range(3 if vz else 2)]
+    return (x, y, *v)
+
+
+def _run(arrs, n, pinned, lean, steps, vz=False):
+    old = os.environ.get("PIC_STAGE_MAX_BYTES")
+    if lean:
+        os.environ["PIC_STAGE_MAX_BYTES"] = "1"
+    try:
+        cfg, q, m = normalized_electrons(NX, NY, 8.0, 6.0, n, 0.05, sort_every=7)
+        cfg.species[0] = P.species(n + 37, q, m, -1, P.SPECIES_HAS_VZ if vz else 0)
+        src = [torch.from_numpy(a).pin_memory().numpy() if pinned else a for a in arrs]
+        with P.Handle(cfg) as h:
+            h.set_particles(0, *src)
+            raw = h.get_particles_raw(0)
+            first = h.get_particles(0, vz=vz)
+            h.prime_leapfrog()
+            h.step(steps)
+            d = h.diagnostics()
+            out = h.get_particles(0, vz=vz)
+            assert d.error_flags == 0
+            assert d.total_charge_fixed == d.expected_charge_fixed
+            return raw, first, out, d.field_energy
+    finally:
+        if old is None:
+            os.environ.pop("PIC_STAGE_MAX_BYTES", None)
+        else:
+            os.environ["PIC_STAGE_MAX_BYTES"] = old
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("vz", [False, True])
+def test_record_and_per_field_paths_agree(pinned, vz):
+    n = NX * NY * 9 + 3  # not a multiple of 4: padded tail slots
+    arrs = _particles(n, 11, vz)
+    rec = _run(arrs, n, pinned, lean=False, steps=20, vz=vz)
+    lean = _run(arrs, n, pinned, lean=True, steps=20, vz=vz)
+    for k in rec[0]:
+        np.testing.assert_array_equal(rec[0][k], lean[0][k], err_msg="sorted " + k)
+    for k in rec[1]:
+        np.testing.assert_array_equal(rec[1][k], lean[1][k], err_msg="export " + k)
+        np.testing.assert_array_equal(rec[2][k], lean[2][k], err_msg="after steps " + k)
+    assert rec[3] == lean[3]
+    # the import keeps every particle, in cell-key order, and the export
+    # returns them in id (input) order
+    cells = rec[0]["cell"][:n]
+    assert np.all(cells >= 0)
+    assert np.array_equal(np.sort(rec[0]["pid"][:n]), np.arange(n, dtype=np.uint32))
+    dx, dy = 8.0 / NX, 6.0 / NY
+    assert np.abs(rec[1]["x"] - arrs[0]).max() < 1e-6 * dx + 1e-12
+    assert np.abs(rec[1]["y"] - arrs[1]).max() < 1e-6 * dy + 1e-12
+    np.testing.assert_array_equal(rec[1]["vx"], arrs[2].astype(np.float32).astype(np.float64))
+    if vz:
+        np.testing.assert_array_equal(rec[1]["vz"], arrs[4].astype(np.float32).astype(np.float64))
