@@ -733,36 +733,51 @@ pic_status pic_get_particles(pic_handle *h, int s, long long *n, double *x, doub
     if (n) *n = cnt;
     const size_t nn = (size_t)cnt;
     if (!nn) return PIC_OK;
-    // id order: the slots' fields scattered as one 32-byte record per id
-    // (or, when the stage cannot hold the records, through the inverse of
-    // the id permutation), then each field converted with coalesced writes
-    // and copied to the host on the copy stream while the next one is
-    // converted
+    // id order: the slots' fields scattered as one 32-byte record per id,
+    // EXPORT_PARTS id ranges at a time for large counts (or, when the stage
+    // cannot hold the records, through the inverse of the id permutation);
+    // each field is converted with coalesced writes and copied to the host
+    // on the copy stream while the next one is prepared
+    double *host[5] = {x, y, vx, vy, vz};
+    int nreq = 0;
+    for (double *p : host) nreq += p != nullptr;
     const size_t cap = (size_t)h->sp[s].cap;
-    const size_t packed_bytes = nn * (32 + 5 * sizeof(double));
+    const int parts = (long long)nn >= EXPORT_SPLIT_MIN ? EXPORT_PARTS : 1;
+    const size_t part_max = (nn + parts - 1) / parts;
+    const size_t packed_bytes = part_max * 32 + nn * nreq * sizeof(double);
     const bool packed = stage_fits(h, packed_bytes);
-    PIC_TRY(ensure_stage(h, packed ? packed_bytes : nn * 5 * sizeof(double) + cap * sizeof(uint32_t)));
+    PIC_TRY(ensure_stage(h, packed ? packed_bytes : nn * nreq * sizeof(double) + cap * sizeof(uint32_t)));
     // packed: records (16-byte aligned) then the doubles; else the doubles
     // then the inverse permutation
     uint4 *rec = (uint4 *)h->stage;
-    double *d = packed ? (double *)(rec + 2 * nn) : (double *)h->stage;
-    uint32_t *inv = (uint32_t *)(d + 5 * nn);
+    double *d = packed ? (double *)(rec + 2 * part_max) : (double *)h->stage;
+    uint32_t *inv = (uint32_t *)(d + nreq * nn);
     if (!h->copy_stream) {
         PIC_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
         for (auto &e : h->field_ready) PIC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         PIC_CUDA(cudaEventCreateWithFlags(&h->copies_done, cudaEventDisableTiming));
     }
-    double *host[5] = {x, y, vx, vy, vz};
     double *dev[5];
-    for (int k = 0; k < 5; ++k) dev[k] = host[k] ? d + k * nn : nullptr;
-    if (packed)
-        PIC_TRY(launch_to_global_by_record(h, s, dev, rec, h->field_ready));
-    else
+    for (int k = 0, j = 0; k < 5; ++k) dev[k] = host[k] ? d + (j++) * nn : nullptr;
+    if (packed) {
+        for (int r = 0; r < parts; ++r) {
+            const long long lo = (long long)(nn * r / parts), hi = (long long)(nn * (r + 1) / parts);
+            cudaEvent_t *ready = h->field_ready + 5 * r;
+            PIC_TRY(launch_to_global_by_record(h, s, lo, hi, dev, rec, ready));
+            for (int k = 0; k < 5; ++k) {
+                if (!host[k] || hi <= lo) continue;
+                PIC_CUDA(cudaStreamWaitEvent(h->copy_stream, ready[k], 0));
+                PIC_CUDA(cudaMemcpyAsync(host[k] + lo, dev[k] + lo, (size_t)(hi - lo) * 8,
+                                         cudaMemcpyDeviceToHost, h->copy_stream));
+            }
+        }
+    } else {
         PIC_TRY(launch_to_global_by_id(h, s, dev, inv, h->field_ready));
-    for (int k = 0; k < 5; ++k) {
-        if (!host[k]) continue;
-        PIC_CUDA(cudaStreamWaitEvent(h->copy_stream, h->field_ready[k], 0));
-        PIC_CUDA(cudaMemcpyAsync(host[k], dev[k], nn * 8, cudaMemcpyDeviceToHost, h->copy_stream));
+        for (int k = 0; k < 5; ++k) {
+            if (!host[k]) continue;
+            PIC_CUDA(cudaStreamWaitEvent(h->copy_stream, h->field_ready[k], 0));
+            PIC_CUDA(cudaMemcpyAsync(host[k], dev[k], nn * 8, cudaMemcpyDeviceToHost, h->copy_stream));
+        }
     }
     PIC_CUDA(cudaEventRecord(h->copies_done, h->copy_stream));
     PIC_CUDA(cudaStreamWaitEvent(h->stream, h->copies_done, 0));

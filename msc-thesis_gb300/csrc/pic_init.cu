@@ -176,35 +176,35 @@ __global__ void id_gather_kernel(const uint32_t *__restrict__ inv, const long lo
     }
 }
 
-// Export through packed records: every slot's fields scattered to the
-// record of its id, {cell, ox, oy, vx}, {vy, vz, cell, 0}, one 32-byte
-// sector per particle written whole.  Records of ids no slot carries keep
-// the 0xFF fill (cell -1).
+// Export through packed records, ids [lo, hi) at a time: every slot whose
+// id falls in the range scatters its fields to that id's record, {cell, ox,
+// oy, vx}, {vy, vz, cell, 0}, one 32-byte sector per particle written whole.
+// Records of ids no slot carries keep the 0xFF fill (cell -1).
 __global__ void id_record_kernel(const int32_t *__restrict__ cell, const float *__restrict__ ox,
                                  const float *__restrict__ oy, const float *__restrict__ vx,
                                  const float *__restrict__ vy, const float *__restrict__ vz,
-                                 const uint32_t *__restrict__ pid, const long long *d_n,
-                                 uint4 *__restrict__ rec)
+                                 const uint32_t *__restrict__ pid, const long long *d_n, long long lo,
+                                 long long hi, uint4 *__restrict__ rec)
 {
     const long long n = *d_n;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const size_t p = pid[i];
-        if ((long long)p >= n) continue;
+        const long long p = pid[i];
+        if (p < lo || p >= hi || p >= n) continue;
+        const size_t r = 2 * (size_t)(p - lo);
         const uint32_t c = (uint32_t)cell[i];
-        rec[2 * p] = make_uint4(c, __float_as_uint(ox[i]), __float_as_uint(oy[i]), __float_as_uint(vx[i]));
-        rec[2 * p + 1] = make_uint4(__float_as_uint(vy[i]), vz ? __float_as_uint(vz[i]) : 0u, c, 0u);
+        rec[r] = make_uint4(c, __float_as_uint(ox[i]), __float_as_uint(oy[i]), __float_as_uint(vx[i]));
+        rec[r + 1] = make_uint4(__float_as_uint(vy[i]), vz ? __float_as_uint(vz[i]) : 0u, c, 0u);
     }
 }
 
-// One exported field in id order from the records (coalesced both ways).
-// field: 0 x, 1 y, 2 vx, 3 vy, 4 vz.
-__global__ void id_record_field_kernel(const uint4 *__restrict__ rec, const long long *d_n, int field,
+// One exported field of `count` consecutive ids from their records
+// (coalesced both ways).  field: 0 x, 1 y, 2 vx, 3 vy, 4 vz.
+__global__ void id_record_field_kernel(const uint4 *__restrict__ rec, long long count, int field,
                                        double d, double *__restrict__ out)
 {
-    const long long n = *d_n;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < count; p += stride) {
         if (field <= 2) {
             const uint4 a = rec[2 * p];
             const int c = (int)a.x;
@@ -421,20 +421,21 @@ pic_status launch_to_global_by_id(pic_handle *h, int s, double *const *out, uint
     return PIC_OK;
 }
 
-pic_status launch_to_global_by_record(pic_handle *h, int s, double *const *out, uint4 *rec,
-                                      cudaEvent_t *ready)
+pic_status launch_to_global_by_record(pic_handle *h, int s, long long lo, long long hi,
+                                      double *const *out, uint4 *rec, cudaEvent_t *ready)
 {
     SpeciesBuf &B = h->sp[s];
-    if (B.cap == 0) return PIC_OK;
+    if (B.cap == 0 || hi <= lo) return PIC_OK;
     const long long *d_n = &h->dev->n[s];
-    PIC_CUDA(cudaMemsetAsync(rec, 0xFF, 32 * (size_t)B.n, h->stream));
+    PIC_CUDA(cudaMemsetAsync(rec, 0xFF, 32 * (size_t)(hi - lo), h->stream));
     id_record_kernel<<<grid_for(B.cap, 256), 256, 0, h->stream>>>(
-        B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.vz[0], B.pid[0], d_n, rec);
+        B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.vz[0], B.pid[0], d_n, lo, hi, rec);
     PIC_CUDA(cudaGetLastError());
     const double dd[5] = {h->g.dx, h->g.dy, 0.0, 0.0, 0.0};
     for (int k = 0; k < 5; ++k) {
         if (!out[k]) continue;
-        id_record_field_kernel<<<grid_for(B.n, 256), 256, 0, h->stream>>>(rec, d_n, k, dd[k], out[k]);
+        id_record_field_kernel<<<grid_for(hi - lo, 256), 256, 0, h->stream>>>(rec, hi - lo, k, dd[k],
+                                                                              out[k] + lo);
         PIC_CUDA(cudaGetLastError());
         PIC_CUDA(cudaEventRecord(ready[k], h->stream));
     }

@@ -94,6 +94,11 @@ struct SpeciesBuf {
     long long nchunks = 0;      // push grid size for this species
 };
 
+// An export of at least EXPORT_SPLIT_MIN particles is done in EXPORT_PARTS
+// id ranges, each copied to the host while the next one is prepared.
+constexpr int EXPORT_PARTS = 4;
+constexpr long long EXPORT_SPLIT_MIN = 1ll << 22;
+
 // Device-side accumulators and counters (one struct in device memory).
 // Block-level partial sums go to one of ACC_SLOTS copies (block index mod
 // ACC_SLOTS) so that the blocks of a kernel, which finish together, do not
@@ -185,7 +190,7 @@ struct pic_handle {
     size_t cub_temp_bytes = 0;
     // export: copies to the host on their own stream, field by field
     cudaStream_t copy_stream = nullptr;
-    cudaEvent_t field_ready[5] = {};
+    cudaEvent_t field_ready[5 * pic::EXPORT_PARTS] = {};
     cudaEvent_t copies_done = nullptr;
 };
 
@@ -223,8 +228,9 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
                               const double *vz_dev);
 pic_status launch_to_global_by_id(pic_handle *h, int s, double *const *out, uint32_t *inv,
                                   cudaEvent_t *ready);
-pic_status launch_to_global_by_record(pic_handle *h, int s, double *const *out, uint4 *rec,
-                                      cudaEvent_t *ready);
+// ids [lo, hi) of an export through packed records (rec holds hi - lo)
+pic_status launch_to_global_by_record(pic_handle *h, int s, long long lo, long long hi,
+                                      double *const *out, uint4 *rec, cudaEvent_t *ready);
 pic_status launch_fill_padding(pic_handle *h, int s, long long from, long long to);
 pic_status launch_init_dA(pic_handle *h, const pic_init_spec *spec, int lat_nx, int lat_ny,
                           double *dxdA, double *dydA);

@@ -24,12 +24,12 @@ def _particles(n, seed, vz=False):
     return (x, y, *v)
 
 
-def _run(arrs, n, pinned, lean, steps, vz=False):
+def _run(arrs, n, pinned, lean, steps, vz=False, nx=NX, ny=NY):
     old = os.environ.get("PIC_STAGE_MAX_BYTES")
     if lean:
         os.environ["PIC_STAGE_MAX_BYTES"] = "1"
     try:
-        cfg, q, m = normalized_electrons(NX, NY, 8.0, 6.0, n, 0.05, sort_every=7)
+        cfg, q, m = normalized_electrons(nx, ny, 8.0, 6.0, n, 0.05, sort_every=7)
         cfg.species[0] = P.species(n + 37, q, m, -1, P.SPECIES_HAS_VZ if vz else 0)
         src = [torch.from_numpy(a).pin_memory().numpy() if pinned else a for a in arrs]
         with P.Handle(cfg) as h:
@@ -74,3 +74,16 @@ def test_record_and_per_field_paths_agree(pinned, vz):
     np.testing.assert_array_equal(rec[1]["vx"], arrs[2].astype(np.float32).astype(np.float64))
     if vz:
         np.testing.assert_array_equal(rec[1]["vz"], arrs[4].astype(np.float32).astype(np.float64))
+
+
+def test_export_in_id_ranges_matches_per_field_export():
+    """From 2^22 particles the record export runs in id ranges, each copied
+    to the host while the next is prepared."""
+    n = (1 << 22) + 5
+    arrs = _particles(n, 12)
+    rec = _run(arrs, n, True, lean=False, steps=3, nx=256, ny=192)
+    lean = _run(arrs, n, True, lean=True, steps=3, nx=256, ny=192)
+    for k in rec[1]:
+        np.testing.assert_array_equal(rec[1][k], lean[1][k], err_msg="export " + k)
+        np.testing.assert_array_equal(rec[2][k], lean[2][k], err_msg="after steps " + k)
+    np.testing.assert_array_equal(rec[1]["vy"], arrs[3].astype(np.float32).astype(np.float64))
