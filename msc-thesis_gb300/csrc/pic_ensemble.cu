@@ -760,8 +760,12 @@ pic_status pic_ensemble_init(pic_ensemble *e, const pic_init_spec *specs)
         uint32_t *scratch = nullptr;
         void *temp = nullptr;
         size_t temp_bytes = 0;
-        PIC_CUDA(cudaMalloc(&scratch, 16 * ns));
-        pic_status s_ = ens_import_sort(e, scratch, &temp, &temp_bytes);
+        // packed records when they fit with 1 GiB to spare
+        size_t free_b = 0, total_b = 0;
+        PIC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const bool packed = free_b >= 48 * ns + (1ull << 30);
+        PIC_CUDA(cudaMalloc(&scratch, (packed ? 48 : 16) * ns));
+        pic_status s_ = ens_import_sort(e, scratch, packed, &temp, &temp_bytes);
         if (s_ == PIC_OK && e->npush) {
             ens_anchor_kernel<<<(e->npush + 255) / 256, 256, 0, st>>>(e->cell[1], e->push_blk,
                                                                       e->d_runs, e->npush, e->anchor);

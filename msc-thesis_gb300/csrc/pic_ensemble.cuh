@@ -106,6 +106,7 @@ pic_status ens_sort(pic_ensemble *E, const float *const *xin = nullptr, float *c
 pic_status ens_graphs(pic_ensemble *E);
 // pic_import.cu: every run, arbitrary order in buffer 0 -> key order in
 // buffer 1; scratch holds 4 words per slot, CUB temporary storage grows in temp
-pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, void **temp, size_t *temp_bytes);
+pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, bool packed, void **temp,
+                           size_t *temp_bytes);
 
 }  // namespace pic

@@ -82,6 +82,16 @@ __global__ void import_pack_kernel(Fields F, long long n, KeyGeo G, unsigned *er
     }
 }
 
+// The records alone (the ensemble's keys come from its own work table).
+__global__ void import_pack_fields_kernel(Fields F, long long n, uint4 *__restrict__ rec)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        rec[2 * i] = make_uint4(F.in[0][i], F.in[1][i], F.in[2][i], F.in[3][i]);
+        rec[2 * i + 1] = make_uint4(F.in[4][i], F.in[5][i], F.nf > 6 ? F.in[6][i] : 0u, 0u);
+    }
+}
+
 // out_f[i] = field f of record src[i]
 __global__ void import_unpack_kernel(Fields F, const uint4 *__restrict__ rec,
                                      const uint32_t *__restrict__ src, long long n)
@@ -183,8 +193,10 @@ pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
 }
 
 // Every run of an ensemble: buffer 0 in arbitrary order -> buffer 1 in key
-// order (anchors are the caller's).
-pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, void **temp, size_t *temp_bytes)
+// order (anchors are the caller's).  `scratch` holds 16 bytes per slot, or
+// 48 with `packed` (the fields then travel as 32-byte records, as above).
+pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, bool packed, void **temp,
+                           size_t *temp_bytes)
 {
     const long long n = E->nslots;
     if (n >= (1ll << 31)) {
@@ -195,8 +207,6 @@ pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, void **temp, size
     import_keys_ens_kernel<<<E->nsort, 256, 0, st>>>(E->cell[0], E->sort_blk, E->d_runs,
                                                       &E->dev[0].err, scratch, scratch + 2 * n);
     PIC_CUDA(cudaGetLastError());
-    const uint32_t *idx = nullptr;
-    PIC_TRY(radix_pairs(scratch, n, key_bits(E->nkeys), temp, temp_bytes, st, &idx));
     Fields F;
     memset(&F, 0, sizeof F);
     const void *in[6] = {E->cell[0], E->ox[0], E->oy[0], E->vx[0], E->vy[0], E->pid[0]};
@@ -206,7 +216,17 @@ pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, void **temp, size
         F.in[f] = (const uint32_t *)in[f];
         F.out[f] = (uint32_t *)out[f];
     }
-    import_gather_kernel<<<grid_for(n, 256), 256, 0, st>>>(F, idx, n);
+    uint4 *rec = reinterpret_cast<uint4 *>(scratch + 4 * n);
+    if (packed) {
+        import_pack_fields_kernel<<<grid_for(n, 256), 256, 0, st>>>(F, n, rec);
+        PIC_CUDA(cudaGetLastError());
+    }
+    const uint32_t *idx = nullptr;
+    PIC_TRY(radix_pairs(scratch, n, key_bits(E->nkeys), temp, temp_bytes, st, &idx));
+    if (packed)
+        import_unpack_kernel<<<grid_for(n, 256), 256, 0, st>>>(F, rec, idx, n);
+    else
+        import_gather_kernel<<<grid_for(n, 256), 256, 0, st>>>(F, idx, n);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }
