@@ -68,7 +68,7 @@ ens_push_kernel(PushArgs A, const SegBlock *__restrict__ blk, const EnsRun *__re
 
 __device__ __forceinline__ KeyGeo run_geo(const EnsRun &R)
 {
-    return KeyGeo{R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off};
+    return key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off);
 }
 
 __global__ void __launch_bounds__(SORT_THREADS)
@@ -492,6 +492,10 @@ SortArgs ens_sort_args(pic_ensemble *E, const float *const *xin, float *const *x
     A.cursor = E->cursor;
     A.nkeys = E->nkeys;
     A.err = &E->dev[0].err;
+    double density = 1e30;  // the sparsest run sizes the window
+    for (const EnsRun &R : E->runs)
+        if (R.n) density = std::min(density, (double)R.n / ((double)R.nx * R.ny));
+    sort_sizes_for(density, &A.wkeys, &A.hbits);
     for (int k = 0; k < 4; ++k) {
         A.xin[k] = xin ? reinterpret_cast<const uint32_t *>(xin[k]) : nullptr;
         A.xout[k] = xout ? reinterpret_cast<uint32_t *>(xout[k]) : nullptr;

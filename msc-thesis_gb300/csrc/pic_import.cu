@@ -39,7 +39,7 @@ __global__ void import_keys_ens_kernel(const int32_t *__restrict__ cell,
 {
     const SegBlock b = blk[blockIdx.x];
     const EnsRun &R = runs[b.run];
-    const KeyGeo G{R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off};
+    const KeyGeo G = key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off);
     for (long long i = b.base + threadIdx.x; i < b.base + b.count; i += blockDim.x) {
         keys[i] = (uint32_t)particle_key(G, err, cell[i]);
         idx[i] = (uint32_t)i;
@@ -162,7 +162,7 @@ pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
     PIC_TRY(ensure_stage(h, (size_t)n * (packed ? 48 : 16)));
     uint32_t *scratch = (uint32_t *)h->stage;
     uint4 *rec = reinterpret_cast<uint4 *>(scratch + 4 * n);
-    const KeyGeo G{g.nx, g.ny, g.tw, g.th, g.ntx, 0};
+    const KeyGeo G = key_geo(g.nx, g.ny, g.tw, g.th, g.ntx, 0);
     Fields F;
     memset(&F, 0, sizeof F);
     const void *in[7] = {B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.pid[0], B.vz[0]};

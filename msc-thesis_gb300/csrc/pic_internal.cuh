@@ -208,6 +208,7 @@ enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s);
+void sort_sizes_for(double density, int *wk, int *hb);
 pic_status scatter_smem_attr(const void *kernel);
 pic_status launch_anchors(pic_handle *h, int s, int buf = 1);
 // pic_import.cu: arbitrary order in buffer 0 -> key order in buffer 0 (records)

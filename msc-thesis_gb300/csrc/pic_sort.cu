@@ -23,6 +23,7 @@
 // and every push chunk knows the tile of its first particle (anchor).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "pic_sort_dev.cuh"
@@ -219,6 +220,21 @@ pic_status launch_anchors(pic_handle *h, int s, int buf)
     return PIC_OK;
 }
 
+// Window keys and log2 hash slots for sort blocks over `density` particles
+// per cell: a window four times the keys a block of sorted particles spans
+// (at least 256, at most SORT_KEYS), a table of half as many slots (128 to
+// HASH_SLOTS) for the particles that left the window's tile rows.
+void sort_sizes_for(double density, int *wk, int *hb)
+{
+    const double span = SORT_CHUNK / std::max(density, 1e-9);
+    int w = 256;
+    while (w < SORT_KEYS && w < 4.0 * span) w *= 2;
+    int b = 7;
+    while ((1 << b) < HASH_SLOTS && (1 << b) < w / 2) ++b;
+    *wk = w;
+    *hb = b;
+}
+
 // Sort species s from buffer 0 into buffer 1 and compute the chunk anchors.
 pic_status launch_sort(pic_handle *h, int s)
 {
@@ -255,6 +271,7 @@ pic_status launch_sort(pic_handle *h, int s)
     A.err = &h->dev->err;
     const long long nkeys = ncell + 1;  // cells + the bin of empty slots
     A.nkeys = nkeys;
+    sort_sizes_for((double)B.n / (double)ncell, &A.wkeys, &A.hbits);
     PIC_CUDA(cudaMemsetAsync(h->count, 0, sizeof(uint32_t) * (size_t)nkeys, h->stream));
     PIC_CUDA(cudaMemsetAsync(B.anchor, 0xFF, sizeof(int32_t) * (size_t)B.nchunks, h->stream));
     const unsigned gp = (unsigned)((B.cap + SORT_CHUNK - 1) / SORT_CHUNK);

@@ -33,18 +33,50 @@ struct SortArgs {
     unsigned int *err;
     const uint32_t *xin[4];  // optional extra per-particle arrays moved along
     uint32_t *xout[4];       // (all four or none)
+    int wkeys, hbits;        // window keys and log2 hash slots in use (0: the maxima)
 };
 
 // Key geometry of the run a sort block works on: the run's grid and tiles
 // and the first key of its range (0 for a single run).  Key key_off + nx*ny
-// is the run's bin of empty slots.
+// is the run's bin of empty slots.  mtw, mth: multipliers that divide a
+// cell coordinate by tw and th (div_coord); 0 divides directly.
 struct KeyGeo {
     int nx, ny, tw, th, ntx, key_off;
+    unsigned mtw, mth;
 };
+
+// m = floor((2^32 - 1) / d) + 1 gives floor(n / d) = umulhi(n, m) for every
+// n < 2^16 and 2 <= d <= 2^16: m = 2^32/d + e with 0 < e <= 1, so n m / 2^32
+// exceeds n/d by less than 2^-16 <= 1/d, less than the gap from n/d to the
+// next integer.  d = 1 gets 0 (n itself).
+__host__ __device__ __forceinline__ unsigned div_magic(int d)
+{
+    return d > 1 ? 0xFFFFFFFFu / (unsigned)d + 1u : 0u;
+}
+
+__host__ __device__ __forceinline__ KeyGeo key_geo(int nx, int ny, int tw, int th, int ntx,
+                                                   int key_off)
+{
+    return KeyGeo{nx, ny, tw, th, ntx, key_off, div_magic(tw), div_magic(th)};
+}
+
+__device__ __forceinline__ int div_coord(int n, int d, unsigned m)
+{
+    return m ? (int)__umulhi((unsigned)n, m) : n / d;
+}
+
+// cell_key with the divisions done by multiplication
+__device__ __forceinline__ int cell_key(int c, const KeyGeo &G)
+{
+    const int cx = c & 0xFFFF, cy = c >> 16;
+    const int tx = div_coord(cx, G.tw, G.mtw), lx = cx - tx * G.tw;
+    const int ty = div_coord(cy, G.th, G.mth), ly = cy - ty * G.th;
+    return ((ty * G.ntx + tx) * G.th + ly) * G.tw + lx;
+}
 
 __device__ __forceinline__ KeyGeo single_geo(const SortArgs &A)
 {
-    return KeyGeo{A.nx, A.ny, A.tw, A.th, A.ntx, 0};
+    return key_geo(A.nx, A.ny, A.tw, A.th, A.ntx, 0);
 }
 
 constexpr int SORT_THREADS = 256;
@@ -56,18 +88,31 @@ constexpr int HASH_PROBES = 8;
 constexpr int HASH_EMPTY = -1;
 constexpr int FALLBACK_BIT = 1 << 30;  // keys are < 2^30
 
-__device__ __forceinline__ unsigned hash_key(int key)
+// Window and table in use by a sort launch: the arrays are sized for the
+// maxima, and a launch over dense data (few keys per block) uses a prefix so
+// that clearing and walking them costs less than its particles.
+struct SortSizes {
+    int wk;  // window keys
+    int hb;  // log2 of the hash slots
+};
+
+__device__ __forceinline__ SortSizes sort_sizes(const SortArgs &A)
 {
-    return ((unsigned)key * 0x9E3779B1u) >> 22;  // top 10 bits: HASH_SLOTS = 1024
+    return SortSizes{A.wkeys ? A.wkeys : SORT_KEYS, A.hbits ? A.hbits : 10};
+}
+
+__device__ __forceinline__ unsigned hash_key(int key, int hb)
+{
+    return ((unsigned)key * 0x9E3779B1u) >> (32 - hb);  // top hb bits
 }
 
 // slot of `key` in the block's table, inserting it if absent; -1 if the
 // bounded probe found no room
-__device__ __forceinline__ int hash_insert(int *tab_key, int key)
+__device__ __forceinline__ int hash_insert(int *tab_key, int key, int hb)
 {
-    const unsigned h = hash_key(key);
+    const unsigned h = hash_key(key, hb);
     for (int p = 0; p < HASH_PROBES; ++p) {
-        const int slot = (int)((h + p) & (HASH_SLOTS - 1));
+        const int slot = (int)((h + p) & ((1u << hb) - 1));
         const int old = atomicCAS(tab_key + slot, HASH_EMPTY, key);
         if (old == HASH_EMPTY || old == key) return slot;
     }
@@ -75,11 +120,11 @@ __device__ __forceinline__ int hash_insert(int *tab_key, int key)
 }
 
 // slot of a key that is already in the table
-__device__ __forceinline__ int hash_find(const int *tab_key, int key)
+__device__ __forceinline__ int hash_find(const int *tab_key, int key, int hb)
 {
-    const unsigned h = hash_key(key);
+    const unsigned h = hash_key(key, hb);
     for (int p = 0; p < HASH_PROBES; ++p) {
-        const int slot = (int)((h + p) & (HASH_SLOTS - 1));
+        const int slot = (int)((h + p) & ((1u << hb) - 1));
         if (tab_key[slot] == key) return slot;
     }
     return 0;  // not reached for keys counted in the table
@@ -96,18 +141,18 @@ __device__ __forceinline__ int particle_key(const KeyGeo &G, unsigned int *err, 
         atomicOr(err, (unsigned)PIC_DEVERR_CELL);
         return empty;
     }
-    return G.key_off + cell_key(c, G.tw, G.th, G.ntx);
+    return G.key_off + cell_key(c, G);
 }
 
 // first key of this block's shared-memory window (block-uniform)
 __device__ __forceinline__ int window_start(const SortArgs &A, const KeyGeo &G, long long base,
-                                            long long end)
+                                            long long end, int wk)
 {
     const long long mid = min(base + SORT_CHUNK / 2, end - 1);
     const int c = A.cin[mid];
     int k = G.key_off;
-    if (c >= 0 && (c & 0xFFFF) < G.nx && (c >> 16) < G.ny) k += cell_key(c, G.tw, G.th, G.ntx);
-    return max(0, k - SORT_KEYS / 2);
+    if (c >= 0 && (c & 0xFFFF) < G.nx && (c >> 16) < G.ny) k += cell_key(c, G);
+    return max(0, k - wk / 2);
 }
 
 // Shared state of one sort block: dense window counts and the straggler table.
@@ -119,10 +164,10 @@ struct SortSmem {
     uint32_t hbase[HASH_SLOTS];
 };
 
-__device__ __forceinline__ void init_smem(SortSmem &S)
+__device__ __forceinline__ void init_smem(SortSmem &S, SortSizes Z)
 {
-    for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) S.cnt[r] = 0u;
-    for (int r = threadIdx.x; r < HASH_SLOTS; r += SORT_THREADS) {
+    for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) S.cnt[r] = 0u;
+    for (int r = threadIdx.x; r < (1 << Z.hb); r += SORT_THREADS) {
         S.hkey[r] = HASH_EMPTY;
         S.hcnt[r] = 0u;
     }
@@ -159,7 +204,7 @@ __device__ __forceinline__ Run warp_run(int key)
 // Pass 1 of both kernels: keys of this thread's particles, counted in the
 // window or the table; a run the table had no room for gets FALLBACK_BIT.
 __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, SortSmem &S,
-                                           long long base, long long end, int k0,
+                                           long long base, long long end, int k0, SortSizes Z,
                                            int (&keys)[SORT_PER_THREAD])
 {
 #pragma unroll
@@ -174,10 +219,10 @@ __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, S
         int fb = 0;
         if (R.head && key >= 0) {
             const unsigned r = (unsigned)(key - k0);
-            if (r < (unsigned)SORT_KEYS) {
+            if (r < (unsigned)Z.wk) {
                 atomicAdd(S.cnt + r, (uint32_t)R.len);
             } else {
-                const int slot = hash_insert(S.hkey, key);
+                const int slot = hash_insert(S.hkey, key, Z.hb);
                 if (slot >= 0)
                     atomicAdd(S.hcnt + slot, (uint32_t)R.len);
                 else
@@ -193,11 +238,12 @@ __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, S
 __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo &G, SortSmem &S,
                                                 long long base, long long end)
 {
-    const int k0 = window_start(A, G, base, end);
-    init_smem(S);
+    const SortSizes Z = sort_sizes(A);
+    const int k0 = window_start(A, G, base, end, Z.wk);
+    init_smem(S, Z);
     __syncthreads();
     int keys[SORT_PER_THREAD];
-    count_keys(A, G, S, base, end, k0, keys);
+    count_keys(A, G, S, base, end, k0, Z, keys);
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
         const Run R = warp_run(keys[j]);
@@ -205,11 +251,11 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
             atomicAdd(A.count + (keys[j] & ~FALLBACK_BIT), (uint32_t)R.len);
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) {
+    for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
         const uint32_t v = S.cnt[r];
         if (v && k0 + r < A.nkeys) atomicAdd(A.count + k0 + r, v);
     }
-    for (int r = threadIdx.x; r < HASH_SLOTS; r += SORT_THREADS)
+    for (int r = threadIdx.x; r < (1 << Z.hb); r += SORT_THREADS)
         if (S.hcnt[r]) atomicAdd(A.count + S.hkey[r], S.hcnt[r]);
 }
 
@@ -263,22 +309,23 @@ __device__ __forceinline__ void stage_fields(ScatterSmem &S, long long base, lon
 __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyGeo &G,
                                                    ScatterSmem &S, long long base, long long end)
 {
-    const int k0 = window_start(A, G, base, end);
-    init_smem(S.s);
+    const SortSizes Z = sort_sizes(A);
+    const int k0 = window_start(A, G, base, end, Z.wk);
+    init_smem(S.s, Z);
     if (threadIdx.x == 0) S.total = 0u;
     __syncthreads();
     int keys[SORT_PER_THREAD];
-    count_keys(A, G, S.s, base, end, k0, keys);
+    count_keys(A, G, S.s, base, end, k0, Z, keys);
     __syncthreads();
     // reserve each distinct key's slice of the output and of the staging order
-    for (int r = threadIdx.x; r < SORT_KEYS; r += SORT_THREADS) {
+    for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
         const uint32_t v = S.s.cnt[r];
         const bool use = v && k0 + r < A.nkeys;
         S.s.base[r] = use ? atomicAdd(A.cursor + k0 + r, v) : 0u;
         S.lbase[r] = use ? atomicAdd(&S.total, v) : 0u;
         S.s.cnt[r] = 0u;
     }
-    for (int r = threadIdx.x; r < HASH_SLOTS; r += SORT_THREADS) {
+    for (int r = threadIdx.x; r < (1 << Z.hb); r += SORT_THREADS) {
         const uint32_t v = S.s.hcnt[r];
         S.s.hbase[r] = v ? atomicAdd(A.cursor + S.s.hkey[r], v) : 0u;
         S.hlbase[r] = v ? atomicAdd(&S.total, v) : 0u;
@@ -295,13 +342,13 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
             if (key & FALLBACK_BIT) {
                 d = atomicAdd(A.cursor + (key & ~FALLBACK_BIT), (uint32_t)R.len);
                 l = atomicAdd(&S.total, (uint32_t)R.len);
-            } else if ((unsigned)(key - k0) < (unsigned)SORT_KEYS) {
+            } else if ((unsigned)(key - k0) < (unsigned)Z.wk) {
                 const int r = key - k0;
                 const uint32_t o = atomicAdd(S.s.cnt + r, (uint32_t)R.len);
                 d = S.s.base[r] + o;
                 l = S.lbase[r] + o;
             } else {
-                const int slot = hash_find(S.s.hkey, key);  // counted in the table in pass 1
+                const int slot = hash_find(S.s.hkey, key, Z.hb);  // counted in the table in pass 1
                 const uint32_t o = atomicAdd(S.s.hcnt + slot, (uint32_t)R.len);
                 d = S.s.hbase[slot] + o;
                 l = S.hlbase[slot] + o;
