@@ -291,12 +291,17 @@ static pic_status copy_back(pic_handle *h, int s)
 // otherwise the periodic counting sort
 static pic_status sort_now(pic_handle *h, bool import = false)
 {
-    for (int s = 0; s < h->cfg.nspecies; ++s) {
-        if (!h->sp[s].cap) continue;
-        bool in0 = false;
-        PIC_TRY(import ? import_sort(h, s, &in0) : launch_sort(h, s));
-        if (!in0) PIC_TRY(copy_back(h, s));
-    }
+    // a species whose import records already sit in the stage goes first
+    // (import_sort consumes the flag, so it is read once up front)
+    bool first[PIC_MAX_SPECIES] = {};
+    for (int s = 0; s < h->cfg.nspecies; ++s) first[s] = h->sp[s].records_ready;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int s = 0; s < h->cfg.nspecies; ++s) {
+            if (!h->sp[s].cap || first[s] != (pass == 0)) continue;
+            bool in0 = false;
+            PIC_TRY(import ? import_sort(h, s, &in0) : launch_sort(h, s));
+            if (!in0) PIC_TRY(copy_back(h, s));
+        }
     h->since_sort = 0;
     return PIC_OK;
 }
@@ -703,8 +708,16 @@ pic_status pic_set_particles(pic_handle *h, int s, long long n, const double *x,
     const double *dvz = vz ? mapped(vz) : nullptr;
     if (n && dx && dy && dvx && dvy && (!vz || dvz)) {
         // page-locked host arrays: the conversion kernel reads them in place
-        // over the CPU-GPU link (coalesced, in particle order)
-        PIC_TRY(launch_from_global(h, s, n, dx, dy, dvx, dvy, dvz));
+        // over the CPU-GPU link (coalesced, in particle order), straight
+        // into the import sort's keys and records when the stage holds them
+        const size_t rec_bytes = (size_t)h->sp[s].cap * 48;
+        if (stage_fits(h, rec_bytes)) {
+            PIC_TRY(ensure_stage(h, rec_bytes));
+            PIC_TRY(launch_from_global_records(h, s, n, dx, dy, dvx, dvy, dvz));
+            h->sp[s].records_ready = true;
+        } else {
+            PIC_TRY(launch_from_global(h, s, n, dx, dy, dvx, dvy, dvz));
+        }
     } else {
         PIC_TRY(ensure_stage(h, std::max<size_t>(1, nn) * 5 * sizeof(double)));
         double *d = (double *)h->stage;
@@ -718,8 +731,10 @@ pic_status pic_set_particles(pic_handle *h, int s, long long n, const double *x,
         PIC_TRY(launch_from_global(h, s, n, d, d + nn, d + 2 * nn, d + 3 * nn,
                                    vz ? d + 4 * nn : nullptr));
     }
-    PIC_TRY(reset_device_state(h));
-    return refresh(h);
+    pic_status rc = reset_device_state(h);
+    if (rc == PIC_OK) rc = refresh(h);
+    h->sp[s].records_ready = false;  // consumed by the import sort, or stale after an error
+    return rc;
 }
 
 pic_status pic_get_particles(pic_handle *h, int s, long long *n, double *x, double *y, double *vx,

@@ -158,8 +158,10 @@ pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
         return PIC_ERR_INVALID_ARG;
     }
     const Geometry &g = h->g;
-    const bool packed = stage_fits(h, (size_t)n * 48);
-    PIC_TRY(ensure_stage(h, (size_t)n * (packed ? 48 : 16)));
+    const bool ready = B.records_ready;  // keys, slots and records written by the conversion
+    B.records_ready = false;
+    const bool packed = ready || stage_fits(h, (size_t)n * 48);
+    if (!ready) PIC_TRY(ensure_stage(h, (size_t)n * (packed ? 48 : 16)));
     uint32_t *scratch = (uint32_t *)h->stage;
     uint4 *rec = reinterpret_cast<uint4 *>(scratch + 4 * n);
     const KeyGeo G = key_geo(g.nx, g.ny, g.tw, g.th, g.ntx, 0);
@@ -173,12 +175,14 @@ pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
         F.in[f] = (const uint32_t *)in[f];
         F.out[f] = (uint32_t *)out[f];
     }
-    if (packed)
+    if (ready) {
+    } else if (packed) {
         import_pack_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(F, n, G, &h->dev->err, scratch,
                                                                     scratch + 2 * n, rec);
-    else
+    } else {
         import_keys_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(B.cell[0], n, G, &h->dev->err,
                                                                     scratch, scratch + 2 * n);
+    }
     PIC_CUDA(cudaGetLastError());
     const uint32_t *idx = nullptr;
     PIC_TRY(radix_pairs(scratch, n, key_bits((long long)g.nx * g.ny + 1), &h->cub_temp,

@@ -11,6 +11,7 @@
 #include <math.h>
 
 #include "pic_internal.cuh"
+#include "pic_sort_dev.cuh"
 
 namespace pic {
 
@@ -120,6 +121,37 @@ __global__ void from_global_kernel(InitArgs A, const double *x, const double *y,
         A.vy[i] = (float)vy[i];
         if (A.vz) A.vz[i] = vz ? (float)vz[i] : 0.f;
         A.pid[i] = (uint32_t)i;
+    }
+}
+
+// Host arrays straight to the import sort's input: for every slot its key
+// and slot number, and its fields as the 32-byte record {cell, ox, oy, vx},
+// {vy, pid, vz, 0}; slots n..cap-1 are empty (cell -1, the empty key).
+__global__ void from_global_records_kernel(InitArgs A, KeyGeo G, long long cap, unsigned *err,
+                                           const double *x, const double *y, const double *vx,
+                                           const double *vy, const double *vz,
+                                           uint32_t *__restrict__ keys, uint32_t *__restrict__ idx,
+                                           uint4 *__restrict__ rec)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
+        idx[i] = (uint32_t)i;
+        if (i < A.n) {
+            int cx, cy;
+            float ox, oy;
+            locate(x[i], A.Lx, A.inv_dx, A.nx, cx, ox);
+            locate(y[i], A.Ly, A.inv_dy, A.ny, cy, oy);
+            const int c = cx | (cy << 16);
+            keys[i] = (uint32_t)particle_key(G, err, c);
+            rec[2 * i] = make_uint4((uint32_t)c, __float_as_uint(ox), __float_as_uint(oy),
+                                    __float_as_uint((float)vx[i]));
+            rec[2 * i + 1] = make_uint4(__float_as_uint((float)vy[i]), (uint32_t)i,
+                                        vz ? __float_as_uint((float)vz[i]) : 0u, 0u);
+        } else {
+            keys[i] = (uint32_t)particle_key(G, err, -1);
+            rec[2 * i] = make_uint4(0xFFFFFFFFu, 0u, 0u, 0u);
+            rec[2 * i + 1] = make_uint4(0u, 0xFFFFFFFFu, 0u, 0u);
+        }
     }
 }
 
@@ -391,6 +423,25 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
                                                                   vz_dev);
         PIC_CUDA(cudaGetLastError());
     }
+    return PIC_OK;
+}
+
+pic_status launch_from_global_records(pic_handle *h, int s, long long n, const double *x_dev,
+                                      const double *y_dev, const double *vx_dev,
+                                      const double *vy_dev, const double *vz_dev)
+{
+    SpeciesBuf &B = h->sp[s];
+    const long long cap = B.cap;
+    if (!cap) return PIC_OK;
+    InitArgs A = base_args(h, s);
+    A.n = n;
+    const Geometry &g = h->g;
+    const KeyGeo G = key_geo(g.nx, g.ny, g.tw, g.th, g.ntx, 0);
+    uint32_t *scratch = (uint32_t *)h->stage;
+    from_global_records_kernel<<<grid_for(cap, 256), 256, 0, h->stream>>>(
+        A, G, cap, &h->dev->err, x_dev, y_dev, vx_dev, vy_dev, vz_dev, scratch, scratch + 2 * cap,
+        reinterpret_cast<uint4 *>(scratch + 4 * cap));
+    PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }
 

@@ -92,6 +92,7 @@ struct SpeciesBuf {
     long long cap = 0;          // allocated slots (multiple of 4)
     long long n = 0;            // host mirror of the count
     long long nchunks = 0;      // push grid size for this species
+    bool records_ready = false; // import keys and records already in the stage
 };
 
 // An export of at least EXPORT_SPLIT_MIN particles is done in EXPORT_PARTS
@@ -227,6 +228,11 @@ pic_status launch_init(pic_handle *h, int s, const pic_init_spec *spec, int lat_
 pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x_dev,
                               const double *y_dev, const double *vx_dev, const double *vy_dev,
                               const double *vz_dev);
+// the same conversion straight into the import sort's stage layout (keys,
+// slots and packed records of all cap slots; see import_sort)
+pic_status launch_from_global_records(pic_handle *h, int s, long long n, const double *x_dev,
+                                      const double *y_dev, const double *vx_dev,
+                                      const double *vy_dev, const double *vz_dev);
 pic_status launch_to_global_by_id(pic_handle *h, int s, double *const *out, uint32_t *inv,
                                   cudaEvent_t *ready);
 // ids [lo, hi) of an export through packed records (rec holds hi - lo)
