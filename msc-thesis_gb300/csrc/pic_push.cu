@@ -245,14 +245,12 @@ size_t push_bulk_smem(const Geometry &g)
     return tma_ring_offset(nw) + (size_t)PIPE_STAGES * 5 * STAGE_PARTICLES * 4;
 }
 
+// set on every launch: the attribute belongs to the current device, and a
+// process may drive several
 template <bool G, bool D> static pic_status bulk_attr(size_t sm)
 {
-    static size_t set = 0;
-    if (sm > set) {
-        PIC_CUDA(cudaFuncSetAttribute(push_kernel_bulk<G, D>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        set = sm;
-    }
+    PIC_CUDA(cudaFuncSetAttribute(push_kernel_bulk<G, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm));
     return PIC_OK;
 }
 
