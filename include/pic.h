@@ -167,12 +167,17 @@ typedef struct pic_init_spec {
 pic_status pic_init_particles(pic_handle *h, int species, const pic_init_spec *spec);
 /* Replace a species' particles from host arrays: positions in [0, L)
  * (global coordinates), velocities; vz may be NULL.  Particle ids are the
- * array indices.  Sorts, deposits and solves for E afterwards. */
+ * array indices.  Sorts, deposits and solves for E afterwards.  Page-locked
+ * arrays are read in place by the GPU; the sort borrows up to 48 bytes of
+ * device memory per slot (16 when less is free or the environment variable
+ * PIC_STAGE_MAX_BYTES caps it; the result is the same). */
 pic_status pic_set_particles(pic_handle *h, int species, long long n, const double *x,
                              const double *y, const double *vx, const double *vy,
                              const double *vz);
 /* Copy a species to host arrays in particle-id order (id i -> index i).
- * *n receives the count; any array may be NULL. */
+ * *n receives the count; any array may be NULL.  Borrows 8 bytes of device
+ * memory per particle and requested array plus 8 per particle for the
+ * reordering (4 per slot under PIC_STAGE_MAX_BYTES or low memory). */
 pic_status pic_get_particles(pic_handle *h, int species, long long *n, double *x, double *y,
                              double *vx, double *vy, double *vz);
 
