@@ -89,7 +89,9 @@ __device__ __forceinline__ void mcc_sigmas(const MccArgs &A, const float *tab, f
     sion = fmaf(f, io[k + 1] - io[k], io[k]);
 }
 
-constexpr int MCC_CHUNK = 2048;  // electrons tested per block pass
+constexpr int MCC_THREADS = 256;
+constexpr int MCC_PER_THREAD = 8;
+constexpr int MCC_CHUNK = MCC_THREADS * MCC_PER_THREAD;  // electrons tested per block pass
 
 // Collision of candidate electron i (r: its first draw of this pass):
 // real (elastic, excitation, ionisation with ion birth) or null.
@@ -192,8 +194,10 @@ __device__ __forceinline__ void mcc_collide(const MccArgs &A, const float *s_tab
 // candidate test (one Philox draw keyed by particle id and pass) and the
 // candidates (fraction P_null, a few percent) are queued in shared memory,
 // then the block's threads work through the queue together, so the costly
-// collision path runs in full warps instead of one lane per warp.
-__global__ void __launch_bounds__(256) mcc_kernel(MccArgs A)
+// collision path runs in full warps instead of one lane per warp.  A thread
+// loads the cells and ids of all its electrons of a chunk before the first
+// draw, so that their DRAM reads overlap.
+__global__ void __launch_bounds__(MCC_THREADS) mcc_kernel(MccArgs A)
 {
     extern __shared__ float s_tab[];  // 4 ntab table floats, then the candidate queue
     int *s_q = reinterpret_cast<int *>(s_tab + 4 * A.ntab);
@@ -214,11 +218,20 @@ __global__ void __launch_bounds__(256) mcc_kernel(MccArgs A)
          c0 += (long long)gridDim.x * MCC_CHUNK) {
         if (threadIdx.x == 0) s_nq = 0u;
         __syncthreads();
-        for (int k = threadIdx.x; k < MCC_CHUNK; k += blockDim.x) {  // same trip count in a warp
-            const long long i = c0 + k;
+        int cellv[MCC_PER_THREAD];
+        uint32_t pidv[MCC_PER_THREAD];
+#pragma unroll
+        for (int j = 0; j < MCC_PER_THREAD; ++j) {
+            const long long i = c0 + threadIdx.x + j * MCC_THREADS;
+            cellv[j] = i < n ? A.ecell[i] : -1;
+            pidv[j] = i < n ? A.epid[i] : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < MCC_PER_THREAD; ++j) {  // warp-uniform trip count
+            const int k = threadIdx.x + j * MCC_THREADS;
             bool cand = false;
-            if (i < n && A.ecell[i] >= 0) {
-                const U4 r = philox4x32_10(U4{A.epid[i], (uint32_t)pass, 0u, STREAM_MCC}, A.k0, A.k1);
+            if (cellv[j] >= 0) {
+                const U4 r = philox4x32_10(U4{pidv[j], (uint32_t)pass, 0u, STREAM_MCC}, A.k0, A.k1);
                 cand = u01f(r.x) < A.p_null;
             }
             const unsigned m = __ballot_sync(full, cand);
@@ -375,7 +388,7 @@ pic_status launch_mcc(pic_handle *h)
     A.dev = h->dev;
     mcc_prepare_kernel<<<1, 1, 0, h->stream>>>(h->dev, M.e);
     PIC_CUDA(cudaGetLastError());
-    mcc_kernel<<<grid_for(E.cap, MCC_CHUNK), 256,
+    mcc_kernel<<<grid_for(E.cap, MCC_CHUNK), MCC_THREADS,
                  4 * M.ntab * sizeof(float) + MCC_CHUNK * sizeof(int), h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
