@@ -97,7 +97,7 @@ struct SpeciesBuf {
 
 // An export of at least EXPORT_SPLIT_MIN particles is done in EXPORT_PARTS
 // id ranges, each copied to the host while the next one is prepared.
-constexpr int EXPORT_PARTS = 4;
+constexpr int EXPORT_PARTS = 8;
 constexpr long long EXPORT_SPLIT_MIN = 1ll << 22;
 
 // Device-side accumulators and counters (one struct in device memory).
