@@ -105,7 +105,8 @@ pic_status ens_poisson(pic_ensemble *E);
 pic_status ens_sort(pic_ensemble *E, const float *const *xin = nullptr, float *const *xout = nullptr);
 pic_status ens_graphs(pic_ensemble *E);
 // pic_import.cu: every run, arbitrary order in buffer 0 -> key order in
-// buffer 1; scratch holds 4 words per slot, CUB temporary storage grows in temp
+// buffer 1; scratch holds 4 words per slot (12 with packed records), CUB
+// temporary storage grows in temp
 pic_status ens_import_sort(pic_ensemble *E, uint32_t *scratch, bool packed, void **temp,
                            size_t *temp_bytes);
 

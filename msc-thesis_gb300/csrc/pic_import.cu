@@ -6,8 +6,10 @@
 // degenerates to one global atomic and one scattered store per field and
 // particle.  Here the cell keys are sorted as (key, slot) pairs with the
 // CUDA toolkit's radix sort (CUB, a library sort of 32-bit pairs over the
-// key's significant bits only) and the particle fields are then gathered
-// into buffer 1 in key order.  Runs once per import, never in the step.
+// key's significant bits only) and the particle fields then follow in key
+// order: as one 32-byte record per particle fetched with a single sector
+// read, or field by field when memory for the records is short.  Runs once
+// per import, never in the step.
 #include <cuda_runtime.h>
 
 #include <cstring>
