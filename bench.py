@@ -493,6 +493,7 @@ def main():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--tile", type=int, nargs=2, default=(0, 0))
     ap.add_argument("--sort-every", type=int, default=SORT_EVERY)
+    ap.add_argument("--halo", type=int, default=0, help="push window halo in cells (0: the library's)")
     ap.add_argument("--push-variant", type=int, default=0, help="0 auto, 1 direct, 2 bulk copy")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (untimed setup)")
     ap.add_argument("--adjoint-steps", type=int, default=500,
@@ -545,7 +546,7 @@ def main():
     A = L * L
     sp = P.species(N, -A / N, A / N, -1)
     cfg = P.config(NX, NY, L, L, DT, [sp], sort_every=SORT_EVERY, device=local,
-                   chunk=args.chunk, tile_w=args.tile[0], tile_h=args.tile[1],
+                   chunk=args.chunk, tile_w=args.tile[0], tile_h=args.tile[1], halo=args.halo,
                    push_variant=args.push_variant)
     spec = P.init_spec(N, vth=(VTH, VTH, 0), pert_kind=P.PERT_DENSITY, pert_amp=0.01,
                        pert_mx=1, pert_my=1, seed=2024 + rank)

@@ -169,7 +169,10 @@ static pic_status setup_geometry(pic_handle *h)
     g.dx = c.Lx / c.nx;
     g.dy = c.Ly / c.ny;
     g.chunk = c.chunk ? c.chunk : 8192;
-    g.halo = c.halo ? c.halo : 2;
+    // default halo 4 cells (measured at 2048^2 x 32 ppc, sort every 40: 1.203
+    // ms per step against 1.234 with 2, 1.211 with 5 or 6, 1.300 with 8),
+    // less where the window would not fit
+    g.halo = c.halo ? c.halo : 4;
     long long maxcap = 0;
     for (int s = 0; s < c.nspecies; ++s) maxcap = std::max(maxcap, c.species[s].capacity);
     const double ppc = std::max(1.0, (double)maxcap / ((double)c.nx * c.ny));
@@ -178,9 +181,16 @@ static pic_status setup_geometry(pic_handle *h)
     g.th = c.tile_h ? c.tile_h : pick_divisor(c.ny, std::max(1, tcells / g.tw));
     g.ntx = c.nx / g.tw;
     g.nty = c.ny / g.th;
-    g.wcx = 2 * g.tw + 2 * g.halo;
-    g.wcy = g.th + 2 * g.halo;
-    const size_t smem = (size_t)(g.wcx + 1) * (g.wcy + 1) * 16 + 32;
+    auto window = [&] {
+        g.wcx = 2 * g.tw + 2 * g.halo;
+        g.wcy = g.th + 2 * g.halo;
+        return (size_t)(g.wcx + 1) * (g.wcy + 1) * 16 + 32;
+    };
+    size_t smem = window();
+    while (!c.halo && smem > 48 * 1024 && g.halo > 1) {
+        --g.halo;
+        smem = window();
+    }
     if (smem > 48 * 1024) {
         set_error("pic_create: shared-memory window too large; use smaller tiles or halo");
         return PIC_ERR_INVALID_ARG;
