@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) adj_kspace_kernel(const float2 *gh, float
     const long long total = (long long)ny * nh;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int my = (int)(idx / nh), mx = (int)(idx - (long long)my * nh);
+        const int my = (int)idx / nh, mx = (int)idx - my * nh;  // ny nh < 2^31
         ph[idx] = adj_mode(gh[idx], gh[total + idx], mx, my, nx, ny, kx1, ky1, inv_eps0_n, idx == 0);
     }
 }

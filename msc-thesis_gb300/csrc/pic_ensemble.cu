@@ -152,8 +152,8 @@ ens_kspace_kernel(const float2 *__restrict__ rhohat, float2 *__restrict__ ehat,
     float fe = 0.f;
     for (long long j = threadIdx.x; j < b.count; j += blockDim.x) {
         const long long idx = b.base + j;  // local mode index
-        const int my = (int)(idx / R.nh);
-        const int mx = (int)(idx - (long long)my * R.nh);
+        const int my = (int)idx / R.nh;  // a run's modes fit in 32 bits
+        const int mx = (int)idx - my * R.nh;
         const KMode K = kspace_mode(rhohat[R.khoff + idx], mx, my, R.nx, R.ny, R.kx1, R.ky1,
                                     R.inv_eps0_n, idx == 0);
         ehat[R.khoff + idx] = K.ex;

@@ -300,7 +300,7 @@ ens_adj_kspace_kernel(const float2 *__restrict__ ghat, float2 *__restrict__ psih
     const EnsRun &R = runs[b.run];
     for (long long j = threadIdx.x; j < b.count; j += blockDim.x) {
         const long long idx = b.base + j;
-        const int my = (int)(idx / R.nh), mx = (int)(idx - (long long)my * R.nh);
+        const int my = (int)idx / R.nh, mx = (int)idx - my * R.nh;  // a run's modes fit in 32 bits
         psihat[R.khoff + idx] = adj_mode(ghat[R.khoff + idx], ghat[R.khoff + R.nk + idx], mx, my,
                                          R.nx, R.ny, R.kx1, R.ky1, R.inv_eps0_n, idx == 0);
     }

@@ -59,16 +59,15 @@ struct KspaceArgs {
     DevState *dev;
 };
 
+// blocks walk rows of the half spectrum, threads the modes of a row
 __global__ void __launch_bounds__(256) kspace_kernel(KspaceArgs A)
 {
     __shared__ double s_part[8];
     const long long total = (long long)A.ny * A.nh;
     float fe = 0.f;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += stride) {
-        const int my = (int)(idx / A.nh);
-        const int mx = (int)(idx - (long long)my * A.nh);
+    for (int my = blockIdx.x; my < A.ny; my += gridDim.x)
+    for (int mx = threadIdx.x; mx < A.nh; mx += blockDim.x) {
+        const long long idx = (long long)my * A.nh + mx;
         const float2 r = A.rhohat[idx];
         const KMode K = kspace_mode(r, mx, my, A.nx, A.ny, A.kx1, A.ky1, A.inv_eps0_n, idx == 0);
         if (mx == A.tmx && my == A.tmy)
@@ -126,8 +125,7 @@ pic_status launch_kspace(pic_handle *h, bool phi_only, float2 *phihat)
     A.tmx = phi_only ? -1 : h->track_mx;
     A.tmy = phi_only ? -1 : h->track_my;
     A.dev = h->dev;
-    const long long total = (long long)g.ny * g.nh;
-    kspace_kernel<<<grid_for(total, 256), 256, 0, h->stream>>>(A);
+    kspace_kernel<<<grid_for((long long)g.ny * 256, 256), 256, 0, h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }
