@@ -87,3 +87,46 @@ def test_export_in_id_ranges_matches_per_field_export():
         np.testing.assert_array_equal(rec[1][k], lean[1][k], err_msg="export " + k)
         np.testing.assert_array_equal(rec[2][k], lean[2][k], err_msg="after steps " + k)
     np.testing.assert_array_equal(rec[1]["vy"], arrs[3].astype(np.float32).astype(np.float64))
+
+
+@pytest.mark.parametrize("lean", [False, True])
+def test_empty_single_and_full_imports(lean):
+    """0 particles, 1 particle and a full species (count = capacity, a
+    multiple of 4: no padding slot) through both paths."""
+    old = os.environ.get("PIC_STAGE_MAX_BYTES")
+    if lean:
+        os.environ["PIC_STAGE_MAX_BYTES"] = "1"
+    try:
+        cap = NX * NY * 4
+        cfg, q, m = normalized_electrons(NX, NY, 8.0, 6.0, cap, 0.05)
+        with P.Handle(cfg) as h:
+            e = np.zeros(0)
+            h.set_particles(0, e, e, e, e)
+            assert h.count(0) == 0
+            h.step(3)
+            a = h.get_particles(0)
+            assert all(len(v) == 0 for v in a.values())
+            d = h.diagnostics()
+            assert d.error_flags == 0 and d.total_charge_fixed == 0
+            one = [np.array([7.9999]), np.array([0.0]), np.array([-0.3]), np.array([0.2])]
+            h.set_particles(0, *one)
+            b = h.get_particles(0)
+            assert abs(b["x"][0] - 7.9999) < 1e-6 and b["y"][0] == 0.0
+            assert b["vx"][0] == np.float32(-0.3) and b["vy"][0] == np.float32(0.2)
+            h.prime_leapfrog()
+            h.step(5)
+            c = h.get_particles(0)
+            assert 0.0 <= c["x"][0] < 8.0 and 0.0 <= c["y"][0] < 6.0
+            arrs = _particles(cap, 13)
+            h.set_particles(0, *arrs)
+            assert h.count(0) == cap
+            f = h.get_particles(0)
+            np.testing.assert_array_equal(f["vy"], arrs[3].astype(np.float32).astype(np.float64))
+            h.step(4)
+            d = h.diagnostics()
+            assert d.error_flags == 0 and d.total_charge_fixed == d.expected_charge_fixed
+    finally:
+        if old is None:
+            os.environ.pop("PIC_STAGE_MAX_BYTES", None)
+        else:
+            os.environ["PIC_STAGE_MAX_BYTES"] = old
