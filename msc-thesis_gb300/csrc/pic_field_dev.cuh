@@ -62,14 +62,15 @@ __device__ __forceinline__ KMode kspace_mode(float2 r, int mx, int my, int nx, i
 // Moves the accumulators of the finished stage into the history ring and
 // clears them; one warp, lane l folds slot l.  ADV_PUSH closes the particle
 // pass of step s (kinetic energy and momentum belong to step s) and advances
-// the step counter; ADV_FIELD records the field of the current step.
+// the step counter; ADV_FIELD records the field of the current step (after
+// the push fold when both bits are set).
 __device__ __forceinline__ void advance_state(DevState *d, double *hist, int cap, int kind,
                                               double fe_scale)
 {
     const int l = threadIdx.x;  // 32 threads = ACC_SLOTS
-    const long long s = d->step;
-    const int k = (int)(s % cap);
-    if (kind == ADV_PUSH) {
+    long long s = d->step;
+    int k = (int)(s % cap);
+    if (kind & ADV_PUSH) {
         const double ke = warp_sum_d(d->ke[l]), px = warp_sum_d(d->px[l]), py = warp_sum_d(d->py[l]);
         d->ke[l] = d->px[l] = d->py[l] = 0.0;
         if (l == 0) {
@@ -78,7 +79,9 @@ __device__ __forceinline__ void advance_state(DevState *d, double *hist, int cap
             hist[3 * (size_t)cap + k] = py;
             d->step = s + 1;
         }
-    } else {
+        k = (int)(++s % cap);
+    }
+    if (kind & ADV_FIELD) {
         const double fe = warp_sum_d(d->fe[l]);
         const unsigned long long q = warp_sum_u64(d->q[l]);
         d->fe[l] = 0.0;

@@ -233,20 +233,22 @@ static void update_mean(pic_handle *h)
 }
 
 // ---------------------------------------------------------------- stages
-pic_status record_poisson(pic_handle *h)
+// adv: the diagnostics folds to launch after the solve (ADV_FIELD, or
+// ADV_PUSH | ADV_FIELD when the particle pass left its fold to this launch)
+pic_status record_poisson(pic_handle *h, int adv)
 {
     PIC_TRY(launch_convert(h));
     PIC_CUFFT(cufftExecR2C(h->plan_r2c, h->rho, (cufftComplex *)h->rhohat));
     PIC_TRY(launch_kspace(h, false, nullptr));
     PIC_CUFFT(cufftExecC2R(h->plan_c2r2, (cufftComplex *)h->ehat, h->e));
-    PIC_TRY(launch_advance(h, ADV_FIELD));
+    PIC_TRY(launch_advance(h, adv));
     return PIC_OK;
 }
 
 // Particle pass of one step.  src = 1: every species was just sorted into
 // buffer 1.  A DSMC species is sorted every step and collides on its sorted
 // buffer before its push moves it back; MCC follows the push.
-pic_status record_push_all(pic_handle *h, int src, bool deposit)
+pic_status record_push_all(pic_handle *h, int src, bool deposit, bool fold)
 {
     for (int s = 0; s < h->cfg.nspecies; ++s) {
         if (!h->sp[s].cap) continue;
@@ -258,15 +260,18 @@ pic_status record_push_all(pic_handle *h, int src, bool deposit)
         }
         PIC_TRY(launch_push(h, s, from, deposit, 1.0f));
     }
-    PIC_TRY(launch_advance(h, ADV_PUSH));
+    if (fold) PIC_TRY(launch_advance(h, ADV_PUSH));
     if (h->mcc.on) PIC_TRY(launch_mcc(h));
     return PIC_OK;
 }
 
+// One step.  Without MCC (whose pass starts from the folded counts) the
+// particle pass's fold rides on the field's: one launch fewer per step.
 static pic_status record_step(pic_handle *h, int src)
 {
-    PIC_TRY(record_push_all(h, src, true));
-    PIC_TRY(record_poisson(h));
+    const bool merge = !h->mcc.on;
+    PIC_TRY(record_push_all(h, src, true, !merge));
+    PIC_TRY(record_poisson(h, merge ? (ADV_PUSH | ADV_FIELD) : ADV_FIELD));
     return PIC_OK;
 }
 

@@ -262,8 +262,8 @@ pic_status launch_to_global_target(const InitTarget &T, const long long *d_n, lo
 int grid_for(long long n, int block);
 
 // pic_handle.cu stages used by other host files
-pic_status record_poisson(pic_handle *h);
-pic_status record_push_all(pic_handle *h, int src, bool deposit);
+pic_status record_poisson(pic_handle *h, int adv = ADV_FIELD);
+pic_status record_push_all(pic_handle *h, int src, bool deposit, bool fold = true);
 pic_status deposit_now(pic_handle *h);
 pic_status refresh(pic_handle *h);
 pic_status ensure_stage(pic_handle *h, size_t bytes);
