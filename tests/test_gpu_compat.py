@@ -41,8 +41,11 @@ def test_compat_run_counts_steps_like_reference(path):
     p, z = case(path)
     xo, yo, sec = P.compat_run(p, z["x0"], z["y0"], z["vx0"], z["vy0"])
     ref = P.compat_run_steps(p, z["x0"], z["y0"], z["vx0"], z["vy0"], int(z["loop_steps"]))
-    np.testing.assert_array_equal(xo, ref["x"])
-    np.testing.assert_array_equal(yo, ref["y"])
+    # two GPU runs agree to the last bits only: the FP64 deposit atomics sum
+    # in scheduling order; one step more or less would move particles by
+    # v dt, orders of magnitude above this tolerance
+    np.testing.assert_allclose(xo, ref["x"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(yo, ref["y"], rtol=0, atol=1e-9)
     assert sec > 0
 
 
