@@ -93,6 +93,8 @@ def test_config1_full_run_conserves_energy_and_charge():
         fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
         ke = h.history(P.HIST_KINETIC, 0, nst)
         qh = h.history(P.HIST_CHARGE, 0, nst + 1)
+        pxh = h.history(P.HIST_MOMENTUM_X, 0, nst)
+        pyh = h.history(P.HIST_MOMENTUM_Y, 0, nst)
         grids = [h.grid(k) for k in (P.GRID_RHO, P.GRID_PHI, P.GRID_EX, P.GRID_EY)]
         d = h.diagnostics()
     tot = fe[:-1] + ke
@@ -102,4 +104,12 @@ def test_config1_full_run_conserves_energy_and_charge():
     # the instability grows and saturates: field energy rises by orders of magnitude
     assert fe.max() > 50 * fe[0]
     assert (qh == -N * 2.0**32).all() and d.error_flags == 0
+    # momentum: the gather and the deposit share the CIC weights and the
+    # spectral gradient is antisymmetric, so the field exerts no net force up
+    # to the deposit's 2^-16 offset quantisation and rounding; drift measured
+    # against one beam's momentum m N/2 v_beam
+    pbeam = m * N / 2 * 0.2
+    dpx, dpy = np.ptp(pxh) / pbeam, np.ptp(pyh) / pbeam
+    print(f"momentum drift over 1000 steps: x {dpx:.2e}, y {dpy:.2e} of one beam's")
+    assert dpx < 1e-6 and dpy < 1e-6  # measured 3.7e-8 and 4.1e-9
     assert all(np.isfinite(g).all() for g in grids)
