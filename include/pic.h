@@ -125,8 +125,11 @@ typedef struct pic_config {
     int history;         /* diagnostic history length in steps (0: 4096)      */
     int device;          /* CUDA device ordinal                               */
     int push_variant;    /* 0: auto (1), 1: direct 128-bit loads, 2: bulk-copy
-                            pipeline, 3: direct loads with deposit groups
-                            summed across the warp                           */
+                            pipeline with block-wide stages, 3: direct loads
+                            with deposit groups summed across the warp,
+                            4: bulk-copy pipeline, one producer warp and
+                            consumer warps on mbarriers (2 and 4 need chunk
+                            a multiple of 1024)                               */
 } pic_config;
 
 typedef struct pic_handle pic_handle;

@@ -197,13 +197,15 @@ static pic_status setup_geometry(pic_handle *h)
     }
     // the bulk-copy pipeline streams whole stages of 1024 particles
     const bool bulk_ok = (g.chunk % 1024) == 0 && push_bulk_smem(g) <= 200 * 1024;
-    if (c.push_variant < 0 || c.push_variant > 3 || (c.push_variant == 2 && !bulk_ok)) {
-        set_error("pic_create: push_variant 2 needs chunk a multiple of 1024 and a smaller window");
+    const bool ws_ok = (g.chunk % 1024) == 0 && push_ws_smem(g) <= 220 * 1024;
+    if (c.push_variant < 0 || c.push_variant > 4 || (c.push_variant == 2 && !bulk_ok) ||
+        (c.push_variant == 4 && !ws_ok)) {
+        set_error("pic_create: push_variant 2 and 4 need chunk a multiple of 1024 and a smaller window");
         return PIC_ERR_INVALID_ARG;
     }
     // measured at 2048^2 x 32 ppc: the direct kernel (1.05 ms) beats the
-    // bulk-copy pipeline (1.27 ms, shared-memory occupancy 3 blocks/SM), so
-    // auto picks direct
+    // bulk-copy pipelines (block-wide stages 1.27 ms; producer and consumer
+    // warps on mbarriers 1.095 ms, 3 blocks per SM), so auto picks direct
     h->use_bulk = (c.push_variant == 2);
     return PIC_OK;
 }

@@ -201,6 +201,7 @@ namespace pic {
 // pic_push.cu
 pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale);
 size_t push_bulk_smem(const Geometry &g);
+size_t push_ws_smem(const Geometry &g);
 pic_status launch_deposit(pic_handle *h, int s);
 // pic_field.cu
 pic_status launch_convert(pic_handle *h);

@@ -201,6 +201,141 @@ __global__ void __launch_bounds__(256) push_kernel_bulk(PushArgs A)
     finish_block<DEPOSIT>(A.geo, W, sAcc, ke, px, py, bad);
 }
 
+// ------------------------------------------------------------------------
+// Warp-specialised pipeline.  One producer warp streams the chunk into a
+// ring of WS_STAGES shared-memory stages of WS_STAGE particles (five
+// cp.async.bulk copies per stage on the bulk-copy engine, completion counted
+// in bytes on the stage's "full" mbarrier); WS_CONSUMERS consumer warps each
+// wait on a stage's full barrier, push one quad per thread straight from
+// shared memory, store the results to global memory and arrive on the
+// stage's "empty" barrier, which the producer waits on before refilling the
+// slot.  No block-wide barrier inside the loop, so the copies of later
+// stages stay in flight while the consumers compute.  Every wait is bounded:
+// on expiry the block raises PIC_DEVERR_TIMEOUT, waits (bounded) for the
+// copies still in flight into its shared memory and leaves without flushing.
+// ------------------------------------------------------------------------
+constexpr int WS_CONSUMERS = 8;
+constexpr int WS_THREADS = 32 * (WS_CONSUMERS + 1);
+constexpr int WS_STAGE = 4 * 32 * WS_CONSUMERS;  // one quad per consumer thread
+// two stages: 3 blocks (24 consumer warps) per SM at 2048^2 x 32 ppc, 1.095
+// ms per push against 1.277 with three or 1.283 with four stages (2 blocks
+// per SM) and 1.046 for the direct kernel's 32 warps, whose latency hiding
+// the consumers' gather and deposit need more than the copies' depth
+constexpr int WS_STAGES = 2;
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// the window, the diagnostics, full and empty barriers, then the ring
+__host__ __device__ __forceinline__ size_t ws_ring_offset(int nw)
+{
+    return (((size_t)nw * 16 + 32 + 2 * WS_STAGES * 8) + 127) & ~(size_t)127;
+}
+
+template <bool GATHER, bool DEPOSIT>
+__global__ void __launch_bounds__(WS_THREADS) push_kernel_ws(PushArgs A)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const long long n = *A.d_n;
+    const long long base = (long long)blockIdx.x * A.chunk;
+    if (base >= n) return;  // block-uniform
+    const long long n4 = (n + 3) & ~3ll;
+    const long long end = min(base + (long long)A.chunk, n4);
+    const Window W = setup_window(A.geo, smem, A.anchor[blockIdx.x]);
+    double *sAcc = reinterpret_cast<double *>(smem + (size_t)W.nw * 16);
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(smem + (size_t)W.nw * 16 + 32);
+    unsigned long long *empty = full + WS_STAGES;
+    unsigned char *ring = smem + ws_ring_offset(W.nw);
+    const int nstages = (int)((end - base + WS_STAGE - 1) / WS_STAGE);
+    constexpr size_t field_bytes = (size_t)WS_STAGE * 4;
+    constexpr size_t stage_bytes = 5 * field_bytes;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < WS_STAGES; ++k) {
+            mbar_init(full + k, 1u);
+            mbar_init(empty + k, (unsigned)WS_CONSUMERS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    load_window<GATHER, DEPOSIT>(A.geo, W);
+    if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
+    __syncthreads();
+
+    float ke = 0.f, px = 0.f, py = 0.f;
+    bool bad = false, timed_out = false;
+    int issued = 0;
+    if (warp == WS_CONSUMERS) {
+        if (lane == 0) {
+            for (int k = 0; k < nstages; ++k) {
+                const int sl = k % WS_STAGES;
+                if (k >= WS_STAGES) {  // the consumers of stage k - WS_STAGES released the slot
+                    if (!mbar_wait_bounded(empty + sl, (unsigned)((k / WS_STAGES - 1) & 1))) {
+                        timed_out = true;
+                        break;
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                }
+                const long long s0 = base + (long long)k * WS_STAGE;
+                const unsigned bytes = (unsigned)min((long long)WS_STAGE, end - s0) * 4u;  // 16-byte multiple
+                unsigned char *dst = ring + (size_t)sl * stage_bytes;
+                mbar_expect_tx(full + sl, 5u * bytes);
+                bulk_g2s(dst + 0 * field_bytes, A.cin + s0, bytes, full + sl);
+                bulk_g2s(dst + 1 * field_bytes, A.oxin + s0, bytes, full + sl);
+                bulk_g2s(dst + 2 * field_bytes, A.oyin + s0, bytes, full + sl);
+                bulk_g2s(dst + 3 * field_bytes, A.vxin + s0, bytes, full + sl);
+                bulk_g2s(dst + 4 * field_bytes, A.vyin + s0, bytes, full + sl);
+                issued = k + 1;
+            }
+        }
+    } else {
+        const int l = 4 * threadIdx.x;  // this thread's quad in every stage
+        for (int k = 0; k < nstages; ++k) {
+            const int sl = k % WS_STAGES;
+            if (!mbar_wait_bounded(full + sl, (unsigned)((k / WS_STAGES) & 1))) {
+                timed_out = true;
+                break;
+            }
+            const long long s0 = base + (long long)k * WS_STAGE;
+            const int cnt = (int)min((long long)WS_STAGE, end - s0);
+            if (l < cnt) {
+                const unsigned char *st = ring + (size_t)sl * stage_bytes;
+                const int4 c4 = *reinterpret_cast<const int4 *>(st + 0 * field_bytes + 4 * l);
+                const float4 a4 = *reinterpret_cast<const float4 *>(st + 1 * field_bytes + 4 * l);
+                const float4 b4 = *reinterpret_cast<const float4 *>(st + 2 * field_bytes + 4 * l);
+                const float4 u4 = *reinterpret_cast<const float4 *>(st + 3 * field_bytes + 4 * l);
+                const float4 v4 = *reinterpret_cast<const float4 *>(st + 4 * field_bytes + 4 * l);
+                int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+                float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
+                float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
+                push_quad<GATHER, DEPOSIT, false>(A.geo, W, cc, xo, yo, xv, yv, ke, px, py, bad);
+                store_quad(A, s0 + l, cc, xo, yo, xv, yv);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty + sl);
+        }
+    }
+    if (__syncthreads_or(timed_out ? 1 : 0)) {
+        // wait (bounded) for the copies still in flight into this block's
+        // shared memory, report, and leave without flushing partial results
+        if (warp == WS_CONSUMERS && lane == 0) {
+            for (int j = max(0, issued - WS_STAGES); j < issued; ++j)
+                mbar_wait_bounded(full + j % WS_STAGES, (unsigned)((j / WS_STAGES) & 1));
+            atomicOr(&A.geo.dev->err, (unsigned)PIC_DEVERR_TIMEOUT);
+        }
+        return;
+    }
+    finish_block<DEPOSIT>(A.geo, W, sAcc, ke, px, py, bad);
+}
+
+size_t push_ws_smem(const Geometry &g)
+{
+    const int nw = (g.wcx + 1) * (g.wcy + 1);
+    return ws_ring_offset(nw) + (size_t)WS_STAGES * 5 * WS_STAGE * 4;
+}
+
 // Deposit-only pass (after a sort or an import, before the first step):
 // fixed-point CIC straight to the global density, one particle per thread.
 __global__ void __launch_bounds__(256)
@@ -324,6 +459,26 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
         } else {
             PIC_TRY((bulk_attr<false, false>(sm)));
             push_kernel_bulk<false, false><<<grid, block, sm, h->stream>>>(A);
+        }
+    } else if (h->cfg.push_variant == 4) {
+        const size_t sm = push_ws_smem(g);
+        const dim3 wsb(WS_THREADS);
+        auto attr = [&](const void *f) -> pic_status {
+            PIC_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            return PIC_OK;
+        };
+        if (charged && dep) {
+            PIC_TRY(attr((const void *)push_kernel_ws<true, true>));
+            push_kernel_ws<true, true><<<grid, wsb, sm, h->stream>>>(A);
+        } else if (charged) {
+            PIC_TRY(attr((const void *)push_kernel_ws<true, false>));
+            push_kernel_ws<true, false><<<grid, wsb, sm, h->stream>>>(A);
+        } else if (dep) {
+            PIC_TRY(attr((const void *)push_kernel_ws<false, true>));
+            push_kernel_ws<false, true><<<grid, wsb, sm, h->stream>>>(A);
+        } else {
+            PIC_TRY(attr((const void *)push_kernel_ws<false, false>));
+            push_kernel_ws<false, false><<<grid, wsb, sm, h->stream>>>(A);
         }
     } else if (h->cfg.push_variant == 3) {
         // warp-summed deposit groups: measured 5% slower at 2048^2 x 32 ppc

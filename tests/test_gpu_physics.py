@@ -164,3 +164,23 @@ def test_odd_grids_match_fp64_oracle(nx, ny):
     s = st.species[0]
     assert np.abs(periodic_diff(a["x"], s["x"], Lx)).max() < 1e-3 * Lx / nx
     assert np.abs(periodic_diff(a["y"], s["y"], Ly)).max() < 1e-3 * Ly / ny
+
+
+def test_pipelined_push_variants_match_direct_loads():
+    """Bulk-copy pipelines (push_variant 2: block-wide stages; 4: producer
+    warp and consumer warps on mbarriers) give the direct kernel's state bit
+    for bit: 8 stages per block (the 4-slot ring wraps), a partial last
+    stage, sorts every 5 steps."""
+    nx, ny = 64, 32
+    n = nx * ny * 20 + 148
+    states = {}
+    for variant in (1, 2, 4):
+        cfg, _, _ = normalized_electrons(nx, ny, 8.0, 4.0, n, 0.1, sort_every=5, chunk=8192,
+                                         push_variant=variant)
+        states[variant] = run_state(cfg, n, 12, seed=7)
+    for variant in (2, 4):
+        for k in states[1][0]:
+            np.testing.assert_array_equal(states[1][0][k], states[variant][0][k],
+                                          err_msg=f"variant {variant} {k}")
+        np.testing.assert_array_equal(states[1][1], states[variant][1])
+        np.testing.assert_array_equal(states[1][2], states[variant][2])
