@@ -249,11 +249,11 @@ ens_adj_kick_kernel(EnsAdjArgs A, const SegBlock *__restrict__ blk, const EnsRun
     if (!W.on) return;
     __syncthreads();
     const float *sx = reinterpret_cast<const float *>(W.sLo), *sy = reinterpret_cast<const float *>(W.sHi);
-    for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
+    WindowWalk w(W);
+    for (int i = threadIdx.x; i < W.nw; i += blockDim.x, w.next(W)) {
         const float fx = sx[i], fy = sy[i];
         if (fx == 0.f && fy == 0.f) continue;
-        const int gxn = (W.wx0 + i % W.nwx) % nx, gyn = (W.wy0 + i / W.nwx) % ny;
-        const size_t o = (size_t)gyn * nx + gxn;
+        const size_t o = w.node(W, nx, ny);
         if (fx != 0.f) atomicAdd(ggx + o, fx);
         if (fy != 0.f) atomicAdd(ggy + o, fy);
     }

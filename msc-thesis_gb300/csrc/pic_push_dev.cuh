@@ -101,14 +101,47 @@ __device__ __forceinline__ Window setup_window(const PushGeo &A, unsigned char *
     return W;
 }
 
+// Walks the window's nodes i = threadIdx.x, threadIdx.x + blockDim.x, ...
+// with their grid node (gx, gy), advanced incrementally (the divisions run
+// once per thread, not once per node).
+struct WindowWalk {
+    int a, b, da, db;  // window column and row, and their step
+    __device__ __forceinline__ WindowWalk(const Window &W)
+    {
+        db = blockDim.x / W.nwx;
+        da = blockDim.x - db * W.nwx;
+        b = threadIdx.x / W.nwx;
+        a = threadIdx.x - b * W.nwx;
+    }
+    __device__ __forceinline__ void next(const Window &W)
+    {
+        a += da;
+        b += db;
+        if (a >= W.nwx) {
+            a -= W.nwx;
+            ++b;
+        }
+    }
+    // grid node of the current window node (wx0 < nx, wy0 < ny)
+    __device__ __forceinline__ size_t node(const Window &W, int nx, int ny) const
+    {
+        int gx = W.wx0 + a, gy = W.wy0 + b;
+        while (gx >= nx) gx -= nx;
+        while (gy >= ny) gy -= ny;
+        return (size_t)gy * nx + gx;
+    }
+};
+
 template <bool GATHER, bool DEPOSIT>
 __device__ __forceinline__ void load_window(const PushGeo &A, const Window &W)
 {
     if (!W.on) return;
-    for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
-        const int a = i % W.nwx, b = i / W.nwx;
-        const int gx = (W.wx0 + a) % A.nx, gy = (W.wy0 + b) % A.ny;
-        if (GATHER) W.sE[i] = make_float2(A.ex[(size_t)gy * A.nx + gx], A.ey[(size_t)gy * A.nx + gx]);
+    WindowWalk w(W);
+    for (int i = threadIdx.x; i < W.nw; i += blockDim.x, w.next(W)) {
+        if (GATHER) {
+            const size_t g = w.node(W, A.nx, A.ny);
+            W.sE[i] = make_float2(A.ex[g], A.ey[g]);
+        }
         if (DEPOSIT) {
             W.sLo[i] = 0u;
             W.sHi[i] = 0u;
@@ -322,13 +355,10 @@ __device__ __forceinline__ void finish_block(const PushGeo &A, const Window &W, 
         if (any_bad) atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_NAN);
     }
     if (DEPOSIT && W.on) {
-        for (int i = threadIdx.x; i < W.nw; i += blockDim.x) {
+        WindowWalk w(W);
+        for (int i = threadIdx.x; i < W.nw; i += blockDim.x, w.next(W)) {
             const unsigned long long v = ((unsigned long long)W.sHi[i] << 16) + W.sLo[i];
-            if (v) {
-                const int a = i % W.nwx, b = i / W.nwx;
-                const int gx = (W.wx0 + a) % A.nx, gy = (W.wy0 + b) % A.ny;
-                atomicAdd(A.rho + (size_t)gy * A.nx + gx, v * A.qmul);
-            }
+            if (v) atomicAdd(A.rho + w.node(W, A.nx, A.ny), v * A.qmul);
         }
     }
 }
