@@ -46,10 +46,10 @@ SORT_EVERY = 20
 BYTES_PER_PARTICLE = 40
 BYTES_PER_CELL = 60
 # DRAM bytes per particle of one push_kernel launch, measured with ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum = 688.1 + 618.3 MB for
+# (dram__bytes_read.sum + dram__bytes_write.sum = 688.7 + 618.8 MB for
 # 33,554,432 particles at 1024^2, the push kernel's ncu capture);
 # the kernel's traffic grows in proportion to the particles it processes
-TRAFFIC_PER_PARTICLE = (688.1e6 + 618.3e6) / 33554432
+TRAFFIC_PER_PARTICLE = (688.7e6 + 618.8e6) / 33554432
 
 
 def peaks():
