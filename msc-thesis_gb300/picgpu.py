@@ -611,3 +611,44 @@ def field_energy_function(handle: Handle, nsteps: int, every: int = 10):
             return tuple(gJ * g for g in ctx.saved_tensors)
 
     return _FieldEnergy.apply
+
+
+def ensemble_field_energy_function(ensemble: Ensemble, specs, nsteps: int, every: int = 50):
+    """A torch.autograd.Function for the batched runs of `ensemble`:
+    (beam_v, pert_amp), two 1-D tensors with one entry per run, -> J, the
+    final field energy of every run after `nsteps` steps from specs[r] with
+    those two entries replaced.  The forward pass runs pic_ensemble_adjoint,
+    so dJ_r/d beam_v_r and dJ_r/d pert_amp_r come with J; backward scales them
+    by the incoming gradient (each J_r depends on its own run's two entries
+    only).  Values pass through host memory."""
+    import copy
+
+    import torch
+
+    base = [copy.copy(s) for s in specs]
+
+    class _EnsembleFieldEnergy(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, beam_v, pert_amp):
+            bv = beam_v.detach().to("cpu", torch.float64).numpy()
+            pa = pert_amp.detach().to("cpu", torch.float64).numpy()
+            if len(bv) != len(base) or len(pa) != len(base):
+                raise ValueError("one beam_v and one pert_amp per run")
+            run = []
+            for s, b, a in zip(base, bv, pa):
+                t = copy.copy(s)
+                t.beam_v, t.pert_amp = float(b), float(a)
+                run.append(t)
+            out, _ = ensemble.adjoint(run, nsteps, every, gradients=False)
+            J = torch.tensor([o[0] for o in out], dtype=beam_v.dtype, device=beam_v.device)
+            gb = torch.tensor([o[1] for o in out], dtype=beam_v.dtype, device=beam_v.device)
+            ga = torch.tensor([o[2] for o in out], dtype=pert_amp.dtype, device=pert_amp.device)
+            ctx.save_for_backward(gb, ga)
+            return J
+
+        @staticmethod
+        def backward(ctx, gJ):
+            gb, ga = ctx.saved_tensors
+            return gJ * gb, gJ * ga
+
+    return _EnsembleFieldEnergy.apply

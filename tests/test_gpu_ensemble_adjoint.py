@@ -115,3 +115,32 @@ def test_ensemble_adjoint_checkpoint_spacing_and_final_state():
         assert out[6][0][r][0] == out[36][0][r][0]
         for a, b in zip(out[6][1][r], out[36][1][r]):
             assert rel_norm(a, b) < 2e-3
+
+
+def test_torch_binding_of_the_batched_adjoint():
+    """ensemble_field_energy_function: J per run from (beam drift, amplitude)
+    tensors; backward gives the ensemble adjoint's dJ/d(beam), dJ/d(amplitude)
+    scaled by the incoming gradient, run by run."""
+    torch = pytest.importorskip("torch")
+    nst = 12
+    cfgs, specs, _ = setup(RUNS)
+    with P.Ensemble(cfgs) as E:
+        ref, _ = E.adjoint(specs, nst, every=4, gradients=False)
+        f = P.ensemble_field_energy_function(E, specs, nst, every=4)
+        bv = torch.tensor([r[3] for r in RUNS], dtype=torch.float64, requires_grad=True)
+        amp = torch.tensor([r[4] for r in RUNS], dtype=torch.float64, requires_grad=True)
+        J = f(bv, amp)
+        w = torch.tensor([1.0, -2.0, 0.5], dtype=torch.float64)
+        (w * J).sum().backward()
+        # another drift for run 1 changes that run's J only
+        bv2 = bv.detach().clone()
+        bv2[1] += 0.01
+        J2 = f(bv2, amp.detach())
+    # J repeats bit for bit; the gradients to the float scatter atomics'
+    # summation order (3e-8 between two calls), far inside the adjoint's error
+    for r in range(len(RUNS)):
+        assert J[r].item() == ref[r][0]
+        assert bv.grad[r].item() == pytest.approx(w[r].item() * ref[r][1], rel=1e-5)
+        assert amp.grad[r].item() == pytest.approx(w[r].item() * ref[r][2], rel=1e-5)
+    assert J2[0].item() == J[0].item() and J2[2].item() == J[2].item()
+    assert J2[1].item() != J[1].item()
