@@ -170,6 +170,30 @@ def time_cpu(steps, nthreads):
     return n * steps / dt, desc, n
 
 
+def fp64_check(P, cfg, spec, q, m, nsteps):
+    """The benchmarked configuration's field energy against the FP64 oracle
+    (the physics restatement in oracle/, OpenMP on the host cores) from the
+    same loaded particles, over the first nsteps steps (untimed)."""
+    import numpy as np
+
+    import oracle as O
+
+    with P.Handle(cfg) as h:
+        h.init_particles(0, spec)
+        a = h.get_particles(0)
+        st = O.PhysState(cfg.nx, cfg.ny, cfg.Lx, cfg.Ly, cfg.dt, cfg.eps0)
+        st.add_species(a["x"], a["y"], a["vx"], a["vy"], q, m)
+        del a
+        h.prime_leapfrog()
+        h.step(nsteps)
+        fe = h.history(P.HIST_FIELD_ENERGY, 0, nsteps + 1)
+    st.prime(nthreads=0)
+    ref = st.run(nsteps, nthreads=0)
+    rel = np.abs(fe - ref["fe"]) / ref["fe"]
+    return {"steps": nsteps, "field_energy_rel_err_max": float(rel.max()),
+            "oracle": "FP64 restatement of the step on the host cores, same loaded particles"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -622,12 +646,15 @@ def main():
         del hin, hout
 
     cpu = None
+    fp64 = None
     if rank == 0 and world == 1 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         nthreads = os.cpu_count() or 1
         v, desc, _ = time_cpu(2, nthreads)
         cpu = {"value": v, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
                "sample": desc + ", 2 steps"}
+        if args.nx == NX:
+            fp64 = fp64_check(P, cfg, spec, -A / N, A / N, 10)
 
     _, _, since_after_warmup = launches_for(args.warmup, 0, SORT_EVERY)
     launches, sorts_timed, _ = launches_for(args.steps, since_after_warmup, SORT_EVERY)
@@ -652,6 +679,7 @@ def main():
                          "kernel": "push_kernel (fused gather+push+deposit)",
                          "kernel_ms": push_ms},
             "cpu_baseline": cpu,
+            "fp64_check": fp64,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk,
