@@ -248,6 +248,42 @@ def c5_runs(P, seed=0, nruns=64, local=0):
     return cfgs, specs, grids, ppcs
 
 
+def ens_fp64_check(P, cfgs, specs, nsteps, max_particles=8_000_000):
+    """The batched runs' field energy against the FP64 oracle over the first
+    nsteps steps (untimed): every run of at most max_particles particles is
+    advanced in one ensemble, and each is compared with the oracle started
+    from the same load (a single handle's init of the same spec)."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    sel = [i for i, s in enumerate(specs) if int(s.n) <= max_particles]
+    if not sel:
+        return None
+    with P.Ensemble([cfgs[i] for i in sel]) as E:
+        E.init([specs[i] for i in sel])
+        E.step(nsteps)
+        fe = [E.history(j, P.HIST_FIELD_ENERGY, 0, nsteps + 1) for j in range(len(sel))]
+    worst = 0.0
+    for j, i in enumerate(sel):
+        c, sp = cfgs[i], specs[i]
+        q, m = c.species[0].q, c.species[0].m
+        with P.Handle(c) as h:
+            h.init_particles(0, sp)
+            a = h.get_particles(0)
+        st = O.PhysState(c.nx, c.ny, c.Lx, c.Ly, c.dt, c.eps0)
+        st.add_species(a["x"], a["y"], a["vx"], a["vy"], q, m)
+        st.prime(nthreads=0)
+        ref = st.run(nsteps, nthreads=0)
+        worst = max(worst, float(np.max(np.abs(fe[j] - ref["fe"]) / ref["fe"].max())))
+    return {"steps": nsteps, "runs_checked": len(sel),
+            "particles_checked": int(sum(int(specs[i].n) for i in sel)),
+            "field_energy_rel_err_max": worst,
+            "oracle": "FP64 restatement of the step on the host cores, per run; error "
+                      "relative to the run's largest field energy"}
+
+
 def bench_ensemble(args):
     """Ensemble of 64 runs: one batched ensemble against the same runs one at
     a time on single handles (each with its own autotuned chunk and cadence)."""
@@ -343,6 +379,7 @@ def bench_ensemble(args):
                "steps": args.adjoint_steps, "every": args.every, "seconds": el,
                "note": "forward with checkpoints + reversed backward walk, one call",
                "J_run0": res[0][0], "dJ_dbeam_run0": res[0][1], "dJ_damp_run0": res[0][2]}
+    fp64 = ens_fp64_check(P, cfgs, specs, 10) if rank == 0 and not args.no_cpu else None
     cells = int(sum(int(g) * int(g) for g in grids))
     step_bytes = BYTES_PER_PARTICLE * total + BYTES_PER_CELL * cells  # this rank's
     achieved = step_bytes * args.steps / (ms / 1000.0) / 1e9
@@ -368,6 +405,7 @@ def bench_ensemble(args):
                              "tuned": {f"{k[0]}^2x{k[1]}": v for k, v in tuned.items()}},
         "speedup_vs_plain": ens_value / plain_value if plain_value else None,
         "batched_adjoint": adj,
+        "fp64_check": fp64,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "kernel": "whole ensemble step"},
         "cpu_baseline": None, "e2e": None,
