@@ -246,6 +246,9 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
     count_keys(A, G, S, base, end, k0, Z, keys);
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
+        // keys the block's table had no room for (rare): counted straight
+        // to the global histogram, one atomic per run
+        if (!__any_sync(0xffffffffu, keys[j] >= 0 && (keys[j] & FALLBACK_BIT))) continue;
         const Run R = warp_run(keys[j]);
         if (R.head && keys[j] >= 0 && (keys[j] & FALLBACK_BIT))
             atomicAdd(A.count + (keys[j] & ~FALLBACK_BIT), (uint32_t)R.len);
