@@ -198,7 +198,7 @@ __global__ void id_gather_kernel(const uint32_t *__restrict__ inv, const long lo
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
         const uint32_t i = inv[p];
-        if ((long long)i >= n) continue;  // an id no slot carries
+        if ((long long)i >= n || cell[i] < 0) continue;  // an id no live slot carries
         if (field == 0)
             out[p] = ((double)(cell[i] & 0xFFFF) + (double)off[i]) * d;
         else if (field == 1)

@@ -66,3 +66,30 @@ def test_ionisation_beyond_capacity_is_reported():
         h.step(2)  # the step still runs with the full species
         a = h.get_particles(0, vz=True)
         assert len(a["vx"]) == d.n[0]
+        # ion slots the overflow may leave empty (cell -1; an ion slot
+        # reserved whose electron found no room) carry no particle: both
+        # export paths leave the caller's values at those ids and agree on
+        # every other id
+        import ctypes as C
+        import os
+
+        raw = h.get_particles_raw(1)
+        ni = int(d.n[1])
+        empty_ids = raw["pid"][:ni][raw["cell"][:ni] < 0]
+        outs = []
+        for lean in (False, True):
+            old = os.environ.pop("PIC_STAGE_MAX_BYTES", None)
+            if lean:
+                os.environ["PIC_STAGE_MAX_BYTES"] = "1"
+            try:
+                arrs = [np.full(ni, 7.0) for _ in range(4)]
+                cnt = C.c_longlong()
+                h._c("pic_get_particles", 1, C.byref(cnt), *[P._ptr(x) for x in arrs], None)
+            finally:
+                os.environ.pop("PIC_STAGE_MAX_BYTES", None)
+                if old is not None:
+                    os.environ["PIC_STAGE_MAX_BYTES"] = old
+            outs.append(arrs)
+        for k in range(4):
+            np.testing.assert_array_equal(outs[0][k], outs[1][k])
+            assert (outs[0][k][empty_ids] == 7.0).all()
