@@ -223,7 +223,7 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}), flush=True)
 
 
-def c5_runs(P, seed=0, nruns=64, local=0):
+def two_stream_ensemble_runs(P, seed=0, nruns=64, local=0):
     """The batched two-stream ensemble: grids from {64,128,256,512}^2,
     particles per cell from {16,...,256}, beam drift U[0.1, 0.3], x-displacement
     amplitude log-U[1e-4, 1e-2] in mode 1 (k = 0.5, L = 4 pi), vth 0.01,
@@ -301,7 +301,7 @@ def bench_ensemble(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
         pg = dist
-    cfgs, specs, grids, ppcs = c5_runs(P, nruns=args.runs, local=local)
+    cfgs, specs, grids, ppcs = two_stream_ensemble_runs(P, nruns=args.runs, local=local)
     total_all = sum(int(s.n) for s in specs)
     grid_counts = {str(k): int((grids == k).sum()) for k in (64, 128, 256, 512)}
     # the runs shard over ranks with no exchange: each rank advances its share
@@ -420,7 +420,7 @@ T_GAS_EV = K_B * 300.0 / E_CH
 EPS0_SI = 8.8541878128e-12
 
 
-def c3_tables(ntab=256, emin=0.01, emax=1000.0):
+def mcc_cross_sections(ntab=256, emin=0.01, emax=1000.0):
     """256 log-spaced energies 0.01..1000 eV: elastic 5e-20 m^2; excitation
     11.5 eV rising linearly to 2e-20 at 30 eV, then flat; ionisation 15.8 eV
     rising linearly to 3e-20 at 100 eV, then flat."""
@@ -477,7 +477,7 @@ def small_workload(P, kind, local):
     ve, vi = np.sqrt(2.0 * E_CH / M_E), np.sqrt(T_GAS_EV * E_CH / M_I)
     h.init_particles(0, P.init_spec(ne, vth=(ve, ve, ve), seed=5))
     h.init_particles(1, P.init_spec(ne, vth=(vi, vi, vi), seed=6))
-    sel, sexc, sion = c3_tables()
+    sel, sexc, sion = mcc_cross_sections()
     h.set_mcc(0, 1, N_GAS, T_GAS_EV, M_E, M_I, E_CH, 0.01, 1000.0, sel, sexc, sion, 11.5,
               15.8, 9)
     pushed = 2 * ne

@@ -13,7 +13,7 @@ NG = 3.2e21                # background neutral density, m^-3
 TN_EV = KB * 300.0 / E_CH  # 300 K
 
 
-def c3_tables(ntab=256, emin=0.01, emax=1000.0):
+def mcc_cross_sections(ntab=256, emin=0.01, emax=1000.0):
     """256 log-spaced energies 0.01..1000 eV: elastic 5e-20 m^2; excitation
     from 11.5 eV rising linearly to 2e-20 at 30 eV, then flat; ionisation from
     15.8 eV rising linearly to 3e-20 at 100 eV, then flat."""
@@ -27,7 +27,7 @@ def c3_tables(ntab=256, emin=0.01, emax=1000.0):
 def mcc_resolved(dt, seed, ntab=256, emin=0.01, emax=1000.0):
     """The constants pic_set_mcc derives (nu_max, P_null rounded to float as
     the GPU uses them), as a dict for the oracle's orc_mcc_pass."""
-    E, sel, sexc, sion = c3_tables(ntab, emin, emax)
+    E, sel, sexc, sion = mcc_cross_sections(ntab, emin, emax)
     v = np.sqrt(2.0 * E * E_CH / ME)
     st = sel + sexc + sion
     nu_max = NG * 1.0001 * np.max(np.maximum(st[:-1], st[1:]) * v[1:])
@@ -39,8 +39,8 @@ def mcc_resolved(dt, seed, ntab=256, emin=0.01, emax=1000.0):
                 nu_max=float(np.float32(nu_max)), p_null=float(np.float32(p_null)), seed=seed)
 
 
-def set_c3_mcc(h, seed, e=0, i=1):
-    E, sel, sexc, sion = c3_tables()
+def set_tabulated_mcc(h, seed, e=0, i=1):
+    E, sel, sexc, sion = mcc_cross_sections()
     h.set_mcc(e, i, NG, TN_EV, ME, MI, E_CH, 0.01, 1000.0, sel, sexc, sion, 11.5, 15.8, seed)
 
 

@@ -7,7 +7,7 @@ import pytest
 
 import oracle as O
 import picgpu as P
-from collide_util import D_NEUTRAL, E_CH, KB, M_NEUTRAL, ME, MI, NG, TN_EV, set_c3_mcc
+from collide_util import D_NEUTRAL, E_CH, KB, M_NEUTRAL, ME, MI, NG, TN_EV, set_tabulated_mcc
 
 pytestmark = pytest.mark.gpu
 
@@ -85,7 +85,7 @@ def test_dsmc_relaxation_conservation_and_rate():
     assert abs(got - expect) < 0.03 * expect
 
 
-def test_config4_small_dsmc_with_mcc_electrons():
+def test_small_dsmc_with_mcc_electrons():
     """Electrons + ions with MCC and the DSMC neutrals in one step loop
     (the MCC + DSMC workload's species on a 64^2 grid, dt = 1e-11 s)."""
     nx = 64
@@ -104,7 +104,7 @@ def test_config4_small_dsmc_with_mcc_electrons():
         h.init_particles(1, P.init_spec(ne_, vth=(vi, vi, vi), seed=5))
         x, y, vx, vy, vz = bimodal(nn, nx)
         h.set_particles(2, x, y, vx, vy, vz)
-        set_c3_mcc(h, seed=9)
+        set_tabulated_mcc(h, seed=9)
         h.set_dsmc(2, D_NEUTRAL, wn, 1.0, np.pi * D_NEUTRAL ** 2 * 3000.0, 21)
         h.prime_leapfrog()
         h.step(100)

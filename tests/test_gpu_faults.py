@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import picgpu as P
-from collide_util import E_CH, ME, MI, TN_EV, set_c3_mcc
+from collide_util import E_CH, ME, MI, TN_EV, set_tabulated_mcc
 from gpu_util import normalized_electrons
 
 pytestmark = pytest.mark.gpu
@@ -51,7 +51,7 @@ def test_ionisation_beyond_capacity_is_reported():
     with P.Handle(cfg) as h:
         h.init_particles(0, P.init_spec(n, vth=(ve, ve, ve), seed=2))
         h.init_particles(1, P.init_spec(n, vth=(vi, vi, vi), seed=3))
-        set_c3_mcc(h, seed=4)
+        set_tabulated_mcc(h, seed=4)
         for _ in range(20):
             h.collide(P.COLLIDE_MCC)
         with pytest.raises(P.PicError) as ei:

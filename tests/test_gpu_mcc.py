@@ -7,7 +7,7 @@ import pytest
 import oracle as O
 import picgpu as P
 from collide_util import (E_CH, ME, MI, TN_EV, energies_eV, ks_statistic, mcc_resolved,
-                          set_c3_mcc)
+                          set_tabulated_mcc)
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +31,7 @@ def mcc_handle(n, te_eV, dt, nx=32, extra=40000, with_field_species=True):
 def test_mcc_pass_matches_oracle_and_collision_frequency():
     n, dt, seed = 200_000, 1e-10, 7
     with mcc_handle(n, 20.0, dt) as h:
-        set_c3_mcc(h, seed)
+        set_tabulated_mcc(h, seed)
         a0 = h.get_particles(0, vz=True)
         h.collide(P.COLLIDE_MCC)
         h.synchronize()
@@ -69,14 +69,14 @@ def test_mcc_pass_matches_oracle_and_collision_frequency():
 
 
 def O_tables():
-    from collide_util import c3_tables
-    return c3_tables()
+    from collide_util import mcc_cross_sections
+    return mcc_cross_sections()
 
 
 def test_mcc_eedf_after_many_passes_matches_oracle():
     n, dt, seed, passes = 100_000, 1e-10, 3, 100
     with mcc_handle(n, 8.0, dt, extra=60000) as h:
-        set_c3_mcc(h, seed)
+        set_tabulated_mcc(h, seed)
         a0 = h.get_particles(0, vz=True)
         for _ in range(passes):
             h.collide(P.COLLIDE_MCC)
@@ -106,7 +106,7 @@ def test_mcc_eedf_after_many_passes_matches_oracle():
     assert eg.mean() < energies_eV(a0).mean()  # excitation and ionisation cool the tail
 
 
-def test_mcc_inside_the_step_config3_small():
+def test_mcc_inside_the_step_small():
     """Electrons and ions with field and MCC through pic_step (the MCC workload's physics
     on a 64^2 grid): charge exact, collisions happen, no device errors."""
     nx, ppc = 64, 16
@@ -121,7 +121,7 @@ def test_mcc_inside_the_step_config3_small():
     with P.Handle(cfg) as h:
         h.init_particles(0, P.init_spec(n, vth=(ve, ve, ve), seed=5))
         h.init_particles(1, P.init_spec(n, vth=(vi, vi, vi), seed=5))
-        set_c3_mcc(h, seed=9)
+        set_tabulated_mcc(h, seed=9)
         h.prime_leapfrog()
         h.step(200)
         h.synchronize()

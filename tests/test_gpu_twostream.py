@@ -54,17 +54,17 @@ def test_growth_rate_matches_linear_theory(nx, ny, ppc):
     assert amp[sel][-1] / amp[sel][0] > 20  # the mode grew through the window
 
 
-def config1_spec(seed=0):
+def two_stream_128_spec(seed=0):
     # x-displacement of amplitude 1e-3 in mode kx = 0.5, uniform random positions
     return P.init_spec(N, layout=P.LOAD_RANDOM, vth=(0.01, 0.01, 0), beam_v=V0,
                        pert_kind=P.PERT_XDISP, pert_amp=1e-3, pert_mx=1, seed=seed)
 
 
-def test_config1_matches_fp64_oracle_early_phase():
+def test_two_stream_128_matches_fp64_oracle_early_phase():
     cfg, q, m = normalized_electrons(NX, NY, L, L, N, DT, sort_every=10)
     nst = 100
     with P.Handle(cfg) as h:
-        h.init_particles(0, config1_spec())
+        h.init_particles(0, two_stream_128_spec())
         st = oracle_from_handle(h, cfg, q, m)
         h.prime_leapfrog()
         st.prime(nthreads=0)
@@ -83,11 +83,11 @@ def test_config1_matches_fp64_oracle_early_phase():
     np.testing.assert_allclose(ex, ref["ex"], atol=2e-3 * np.abs(ref["ex"]).max())
 
 
-def test_config1_full_run_conserves_energy_and_charge():
+def test_two_stream_128_full_run_conserves_energy_charge_momentum():
     cfg, q, m = normalized_electrons(NX, NY, L, L, N, DT, sort_every=10)
     nst = 1000
     with P.Handle(cfg) as h:
-        h.init_particles(0, config1_spec())
+        h.init_particles(0, two_stream_128_spec())
         h.prime_leapfrog()
         h.step(nst)
         fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
