@@ -372,7 +372,10 @@ enum pic_device_errors {
     PIC_DEVERR_NAN = 1,       /* a particle had a non-finite velocity          */
     PIC_DEVERR_CAPACITY = 2,  /* a species ran out of capacity (ionisation)    */
     PIC_DEVERR_CELL = 4,      /* a cell index outside the grid was seen        */
-    PIC_DEVERR_TIMEOUT = 8    /* a bounded device wait gave up                 */
+    PIC_DEVERR_TIMEOUT = 8,   /* a bounded device wait gave up                 */
+    PIC_DEVERR_SORT = 16      /* a sort destination fell outside the slots
+                                 (cell counts inconsistent with the particles;
+                                 the particle was left unmoved)               */
 };
 
 pic_status pic_diagnostics(pic_handle *h, pic_diag *d);

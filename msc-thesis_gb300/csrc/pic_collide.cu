@@ -267,6 +267,7 @@ struct NtcArgs {
     const uint32_t *offset;   // per key: particles [offset[k], offset[k+1])
     float *sgmax;             // per key (sigma g)_max
     long long nkeys;
+    long long nslots;         // slots of the sorted buffer (bound of the offsets)
     float sigma;              // pi d^2
     float coef;               // F_N dt_c / (2 V_c)
     uint32_t k0, k1;
@@ -284,8 +285,12 @@ __global__ void __launch_bounds__(256) ntc_kernel(NtcArgs A)
     for (long long key = (long long)blockIdx.x * blockDim.x + threadIdx.x; key < A.nkeys;
          key += stride) {
         const uint32_t o0 = A.offset[key], o1 = A.offset[key + 1];
+        if (o1 < o0 || (long long)o1 > A.nslots) {  // offsets that do not fit the slots
+            atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_SORT);
+            continue;
+        }
         const uint32_t n = o1 - o0;
-        if (n < 2 || o1 < o0) continue;
+        if (n < 2) continue;
         float sgm = A.sgmax[key];
         const float want = A.coef * (float)n * (float)(n - 1) * sgm;
         const U4 r0 = philox4x32_10(U4{(uint32_t)key, (uint32_t)pass, 0u, STREAM_DSMC}, A.k0, A.k1);
@@ -406,6 +411,7 @@ pic_status launch_ntc(pic_handle *h)
     A.offset = h->offset;
     A.sgmax = D.sgmax;
     A.nkeys = (long long)h->g.nx * h->g.ny;
+    A.nslots = B.cap;
     A.sigma = D.sigma;
     A.coef = D.coef;
     A.k0 = (uint32_t)D.seed;

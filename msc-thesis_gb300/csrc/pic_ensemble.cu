@@ -63,6 +63,8 @@ ens_push_kernel(PushArgs A, const SegBlock *__restrict__ blk, const EnsRun *__re
     G.qmul = R.qmul;
     G.ke_scale = drift > 0.f ? R.ke_scale : 0.0;
     G.p_scale = R.p_scale;
+    G.recount = nullptr;
+    G.ntx = R.ntx;
     push_block<GATHER, DEPOSIT, false>(A, G, smem, b.base, b.base + b.count, anchor[blockIdx.x]);
 }
 
@@ -492,6 +494,7 @@ SortArgs ens_sort_args(pic_ensemble *E, const float *const *xin, float *const *x
     A.count = E->count;
     A.cursor = E->cursor;
     A.nkeys = E->nkeys;
+    A.nslots = E->nslots;
     A.err = &E->dev[0].err;
     double density = 1e30;  // the sparsest run sizes the window
     for (const EnsRun &R : E->runs)
@@ -701,6 +704,14 @@ pic_status pic_ensemble_synchronize(pic_ensemble *e)
     if (err & PIC_DEVERR_CELL) {
         set_error("device: cell index outside the grid");
         return PIC_ERR_STATE;
+    }
+    if (err & PIC_DEVERR_SORT) {
+        set_error("device: a sort destination fell outside the slots");
+        return PIC_ERR_STATE;
+    }
+    if (err & PIC_DEVERR_TIMEOUT) {
+        set_error("device: a bounded wait gave up");
+        return PIC_ERR_TIMEOUT;
     }
     if (err & PIC_DEVERR_NAN) {
         set_error("device: non-finite particle velocity");

@@ -99,6 +99,7 @@ static void free_handle_buffers(pic_handle *h)
     cudaFree(h->stage);
     cudaFree(h->mcc.tab);
     cudaFree(h->dsmc.sgmax);
+    cudaFree(h->dsmc.count);
     if (h->plan_r2c) cufftDestroy(h->plan_r2c);
     if (h->plan_c2r2) cufftDestroy(h->plan_c2r2);
     if (h->plan_c2r1) cufftDestroy(h->plan_c2r1);
@@ -256,7 +257,7 @@ pic_status record_push_all(pic_handle *h, int src, bool deposit, bool fold)
         if (!h->sp[s].cap) continue;
         int from = src;
         if (h->dsmc.on && s == h->dsmc.s) {
-            if (!src) PIC_TRY(launch_sort(h, s));
+            if (!src) PIC_TRY(launch_sort(h, s, true));  // counts kept by its last push
             PIC_TRY(launch_ntc(h));
             from = 1;
         }
@@ -318,6 +319,7 @@ static pic_status sort_now(pic_handle *h, bool import = false)
             bool in0 = false;
             PIC_TRY(import ? import_sort(h, s, &in0) : launch_sort(h, s));
             if (!in0) PIC_TRY(copy_back(h, s));
+            if (import) PIC_TRY(launch_recount(h, s));  // the DSMC species' kept counts
         }
     h->since_sort = 0;
     return PIC_OK;
@@ -677,6 +679,14 @@ static pic_status check_flags(pic_handle *h)
     if (err & PIC_DEVERR_CELL) {
         set_error("device: a particle cell index outside the grid was found");
         return PIC_ERR_STATE;
+    }
+    if (err & PIC_DEVERR_SORT) {
+        set_error("device: a sort destination fell outside the species' slots");
+        return PIC_ERR_STATE;
+    }
+    if (err & PIC_DEVERR_TIMEOUT) {
+        set_error("device: a bounded wait gave up");
+        return PIC_ERR_TIMEOUT;
     }
     if (err & PIC_DEVERR_CAPACITY) {
         set_error("device: species capacity exceeded");
@@ -1141,9 +1151,12 @@ extern "C" pic_status pic_set_dsmc(pic_handle *h, const pic_dsmc_params *p)
     D.sigma = (float)(3.14159265358979323846 * p->diameter * p->diameter);
     D.coef = (float)(p->weight * h->cfg.dt / (2.0 * h->g.dx * h->g.dy * p->depth));
     D.seed = p->seed;
+    if (!D.count) PIC_CUDA(cudaMalloc(&D.count, (ncell + 1) * sizeof(uint32_t)));
     D.on = true;
     drop_graphs(h);
-    return PIC_OK;
+    // a full sort counts the species into D.count, which its pushes then keep
+    PIC_TRY(launch_sort(h, D.s));
+    return copy_back(h, D.s);
 }
 
 extern "C" pic_status pic_collide(pic_handle *h, int kind)
@@ -1161,7 +1174,7 @@ extern "C" pic_status pic_collide(pic_handle *h, int kind)
             set_error("pic_collide: DSMC not configured (pic_set_dsmc)");
             return PIC_ERR_STATE;
         }
-        PIC_TRY(launch_sort(h, h->dsmc.s));
+        PIC_TRY(launch_sort(h, h->dsmc.s, true));
         PIC_TRY(launch_ntc(h));
         return copy_back(h, h->dsmc.s);
     }

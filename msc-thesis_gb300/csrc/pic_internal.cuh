@@ -135,6 +135,8 @@ struct DsmcState {
     bool on = false;
     int s = 0;
     float *sgmax = nullptr;   // per cell key
+    uint32_t *count = nullptr;  // the species' particles per cell key (and the empty bin),
+                                // recounted by every full sort, kept by its push
     float sigma = 0, coef = 0;
     unsigned long long seed = 0;
 };
@@ -209,7 +211,8 @@ pic_status launch_kspace(pic_handle *h, bool phi_only, float2 *phihat);
 enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
-pic_status launch_sort(pic_handle *h, int s);
+pic_status launch_sort(pic_handle *h, int s, bool counts_kept = false);
+pic_status launch_recount(pic_handle *h, int s);
 void sort_sizes_for(double density, int *wk, int *hb);
 pic_status scatter_smem_attr(const void *kernel);
 pic_status launch_anchors(pic_handle *h, int s, int buf = 1);

@@ -432,6 +432,10 @@ static PushArgs push_args(pic_handle *h, int s, int src, float dt_scale)
     A.geo.qmul = (unsigned long long)(long long)D.q_int;
     A.geo.ke_scale = move ? 0.25 * D.m : 0.0;
     A.geo.p_scale = 0.5 * D.m;
+    // the DSMC species, sorted every step, keeps its cell counts current here
+    // so that its sort can skip the histogram
+    A.geo.recount = (h->dsmc.on && s == h->dsmc.s) ? h->dsmc.count : nullptr;
+    A.geo.ntx = g.ntx;
     return A;
 }
 

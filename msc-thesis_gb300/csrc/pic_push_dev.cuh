@@ -52,7 +52,16 @@ struct PushGeo {
     float qm_dt, dtdx, dtdy;
     unsigned long long qmul;  // q_int as two's complement
     double ke_scale, p_scale; // m/4, m/2 (0 disables the diagnostics)
+    uint32_t *recount;        // per cell key: counts kept current across cell changes (or null)
+    int ntx;                  // tiles along x (cell keys of recount)
 };
+
+// tile-major cell key (the sort's key; divisions, for the rare cell changes)
+__device__ __forceinline__ int push_cell_key(int cx, int cy, const PushGeo &A)
+{
+    const int tx = cx / A.tw, ty = cy / A.th;
+    return ((ty * A.ntx + tx) * A.th + (cy - ty * A.th)) * A.tw + (cx - tx * A.tw);
+}
 
 // Particle arrays of a push pass (and, for a single run, its PushGeo).
 struct PushArgs {
@@ -279,6 +288,10 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
             if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
         }
         const int cn = cx | (cy << 16);
+        if (MOVE && A.recount && cn != c) {  // a particle that changed cells
+            atomicAdd(A.recount + push_cell_key(cx, cy, A), 1u);
+            atomicSub(A.recount + push_cell_key(c & 0xFFFF, c >> 16, A), 1u);
+        }
         cc[j] = cn;
         xo[j] = ox;
         yo[j] = oy;

@@ -235,12 +235,12 @@ void sort_sizes_for(double density, int *wk, int *hb)
     *hb = b;
 }
 
-// Sort species s from buffer 0 into buffer 1 and compute the chunk anchors.
-pic_status launch_sort(pic_handle *h, int s)
+// Arguments of a sort of species s from buffer 0 into buffer 1.  The DSMC
+// species counts into its own array (kept current by its pushes).
+static SortArgs sort_args(pic_handle *h, int s)
 {
     SpeciesBuf &B = h->sp[s];
     const Geometry &g = h->g;
-    if (B.cap == 0) return PIC_OK;
     const long long ncell = (long long)g.nx * g.ny;
     SortArgs A;
     memset(&A, 0, sizeof A);
@@ -258,7 +258,8 @@ pic_status launch_sort(pic_handle *h, int s)
     A.vyout = B.vy[1];
     A.vzout = B.vz[1];
     A.pidout = B.pid[1];
-    A.count = h->count;
+    const bool dsmc = h->dsmc.on && s == h->dsmc.s && h->dsmc.count;
+    A.count = dsmc ? h->dsmc.count : h->count;
     A.cursor = h->cursor;
     A.anchor = B.anchor;
     A.d_n = &h->dev->n[s];
@@ -269,15 +270,44 @@ pic_status launch_sort(pic_handle *h, int s)
     A.ntx = g.ntx;
     A.chunk = g.chunk;
     A.err = &h->dev->err;
-    const long long nkeys = ncell + 1;  // cells + the bin of empty slots
-    A.nkeys = nkeys;
+    A.nkeys = ncell + 1;  // cells + the bin of empty slots
+    A.nslots = B.cap;
     sort_sizes_for((double)B.n / (double)ncell, &A.wkeys, &A.hbits);
-    PIC_CUDA(cudaMemsetAsync(h->count, 0, sizeof(uint32_t) * (size_t)nkeys, h->stream));
+    return A;
+}
+
+// Histogram of species s's buffer 0 into its counts (zeroed first).
+static pic_status launch_hist(pic_handle *h, int s, const SortArgs &A)
+{
+    const SpeciesBuf &B = h->sp[s];
+    PIC_CUDA(cudaMemsetAsync(A.count, 0, sizeof(uint32_t) * (size_t)A.nkeys, h->stream));
+    sort_hist_kernel<<<(unsigned)((B.cap + SORT_CHUNK - 1) / SORT_CHUNK), SORT_THREADS, 0, h->stream>>>(A);
+    PIC_CUDA(cudaGetLastError());
+    return PIC_OK;
+}
+
+// The DSMC species' counts recomputed from its buffer 0 (after a sort that
+// did not count, an import).
+pic_status launch_recount(pic_handle *h, int s)
+{
+    if (!(h->dsmc.on && s == h->dsmc.s && h->dsmc.count) || !h->sp[s].cap) return PIC_OK;
+    return launch_hist(h, s, sort_args(h, s));
+}
+
+// Sort species s from buffer 0 into buffer 1 and compute the chunk anchors.
+// With counts_kept the DSMC species' pushes have kept its counts current since
+// they were last computed, and the histogram is skipped.
+pic_status launch_sort(pic_handle *h, int s, bool counts_kept)
+{
+    SpeciesBuf &B = h->sp[s];
+    if (B.cap == 0) return PIC_OK;
+    const SortArgs A = sort_args(h, s);
+    const bool dsmc = h->dsmc.on && s == h->dsmc.s && h->dsmc.count;
+    const long long nkeys = A.nkeys;
     PIC_CUDA(cudaMemsetAsync(B.anchor, 0xFF, sizeof(int32_t) * (size_t)B.nchunks, h->stream));
     const unsigned gp = (unsigned)((B.cap + SORT_CHUNK - 1) / SORT_CHUNK);
-    sort_hist_kernel<<<gp, SORT_THREADS, 0, h->stream>>>(A);
-    PIC_CUDA(cudaGetLastError());
-    scan_blocks_kernel<<<h->scan_blocks, 1024, 0, h->stream>>>(h->count, h->offset, nkeys, h->bsum);
+    if (!(dsmc && counts_kept)) PIC_TRY(launch_hist(h, s, A));
+    scan_blocks_kernel<<<h->scan_blocks, 1024, 0, h->stream>>>(A.count, h->offset, nkeys, h->bsum);
     PIC_CUDA(cudaGetLastError());
     scan_bsum_kernel<<<1, 1024, 0, h->stream>>>(h->bsum, h->scan_blocks);
     PIC_CUDA(cudaGetLastError());

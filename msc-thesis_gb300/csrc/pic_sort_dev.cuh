@@ -34,6 +34,7 @@ struct SortArgs {
     const uint32_t *xin[4];  // optional extra per-particle arrays moved along
     uint32_t *xout[4];       // (all four or none)
     int wkeys, hbits;        // window keys and log2 hash slots in use (0: the maxima)
+    long long nslots;        // slots of the destination arrays (scatter bound)
 };
 
 // Key geometry of the run a sort block works on: the run's grid and tiles
@@ -87,6 +88,7 @@ constexpr int HASH_SLOTS = 1024;  // power of two
 constexpr int HASH_PROBES = 8;
 constexpr int HASH_EMPTY = -1;
 constexpr int FALLBACK_BIT = 1 << 30;  // keys are < 2^30
+constexpr uint32_t SORT_NO_SLOT = 0xFFFFFFFFu;  // a destination outside the slots
 
 // Window and table in use by a sort launch: the arrays are sized for the
 // maxima, and a launch over dense data (few keys per block) uses a prefix so
@@ -299,6 +301,7 @@ __device__ __forceinline__ void stage_fields(ScatterSmem &S, long long base, lon
     const int total = (int)S.total;
     for (int t = threadIdx.x; t < total; t += SORT_THREADS) {
         const uint32_t d = S.dst[t];
+        if (d == SORT_NO_SLOT) continue;
 #pragma unroll
         for (int f = 0; f < NF; ++f) dst[f][d] = stage[f * SORT_CHUNK + t];
     }
@@ -359,6 +362,10 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
         }
         d = __shfl_sync(0xffffffffu, d, R.hidx) + (uint32_t)R.rank;
         l = __shfl_sync(0xffffffffu, l, R.hidx) + (uint32_t)R.rank;
+        if (key >= 0 && (long long)d >= A.nslots) {  // counts that do not match the particles
+            atomicOr(A.err, (unsigned)PIC_DEVERR_SORT);
+            d = SORT_NO_SLOT;
+        }
         if (key >= 0) S.dst[l] = d;
         keys[j] = key >= 0 ? (int)l : -1;
     }

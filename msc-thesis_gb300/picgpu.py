@@ -28,7 +28,7 @@ PERT_NONE, PERT_XDISP, PERT_DENSITY, PERT_BEAM_MODE = 0, 1, 2, 3
 COLLIDE_MCC, COLLIDE_DSMC = 1, 2
 GRID_RHO, GRID_PHI, GRID_EX, GRID_EY = 0, 1, 2, 3
 HIST_FIELD_ENERGY, HIST_KINETIC, HIST_MOMENTUM_X, HIST_MOMENTUM_Y, HIST_CHARGE, HIST_MODE_AMP = range(6)
-DEVERR_NAN, DEVERR_CAPACITY, DEVERR_CELL = 1, 2, 4
+DEVERR_NAN, DEVERR_CAPACITY, DEVERR_CELL, DEVERR_TIMEOUT, DEVERR_SORT = 1, 2, 4, 8, 16
 
 STATUS = {0: "PIC_OK", 1: "PIC_ERR_INVALID_ARG", 2: "PIC_ERR_OOM", 3: "PIC_ERR_CUDA",
           4: "PIC_ERR_CUFFT", 5: "PIC_ERR_OVERFLOW", 6: "PIC_ERR_NAN", 7: "PIC_ERR_TIMEOUT",

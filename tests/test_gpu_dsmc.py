@@ -59,6 +59,11 @@ def test_dsmc_relaxation_conservation_and_rate():
         c_before = h.collision_counts()
         h.step(20)
         c_after = h.collision_counts()
+        # 220 steps of every-step sorts on cell counts the push keeps current
+        # (0.15 cells of motion per step): every particle still present once
+        raw = h.get_particles_raw(0)
+        assert np.array_equal(np.sort(raw["pid"][:n]), np.arange(n, dtype=np.uint32))
+        assert (raw["cell"][:n] >= 0).all()
     Tg = np.array(Tg)
     p1 = np.array([a["vx"].sum(), a["vy"].sum(), a["vz"].sum()])
     e1 = (a["vx"] ** 2 + a["vy"] ** 2 + a["vz"] ** 2).sum()
