@@ -108,11 +108,10 @@ __global__ void ens_anchor_kernel(const int32_t *__restrict__ cell, const SegBlo
     anchor[i] = (t % R.ntx) | ((t / R.ntx) << 16);
 }
 
-// rho = (rho_fix - mean) * scale per run, exact charge sum per run, rho_fix
-// cleared as it is read.  Nodes in pairs (ncp is a multiple of 4); nodes past
-// nx*ny are padding (never deposited to, so they stay zero).
+// rho = (rho_fix - mean) * scale per run, exact charge sum per run.  Nodes
+// in pairs (ncp is a multiple of 4); nodes past nx*ny are padding.
 __global__ void __launch_bounds__(256)
-ens_convert_kernel(unsigned long long *__restrict__ rho_fix, float *__restrict__ rho,
+ens_convert_kernel(const unsigned long long *__restrict__ rho_fix, float *__restrict__ rho,
                    const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs, DevState *devs)
 {
     __shared__ unsigned long long s_part[8];
@@ -126,7 +125,6 @@ ens_convert_kernel(unsigned long long *__restrict__ rho_fix, float *__restrict__
         const long long node = b.base + j;       // local node index (even)
         const long long g = R.goff + node;
         const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(rho_fix + g);
-        *reinterpret_cast<ulonglong2 *>(rho_fix + g) = make_ulonglong2(0ull, 0ull);
         if (node + 1 < ncell) {
             qs += v.x + v.y;
             *reinterpret_cast<float2 *>(rho + g) =
@@ -460,6 +458,7 @@ pic_status ens_poisson(pic_ensemble *E)
     cudaStream_t st = E->stream;
     ens_convert_kernel<<<E->nnode_blk, 256, 0, st>>>(E->rho_fix, E->rho, E->node_blk, E->d_runs, E->dev);
     PIC_CUDA(cudaGetLastError());
+    PIC_CUDA(cudaMemsetAsync(E->rho_fix, 0, sizeof(unsigned long long) * (size_t)E->nnodes, st));
     for (auto &G : E->groups) {
         const EnsRun &R = E->runs[G.first];
         PIC_CUFFT(cufftExecR2C(G.r2c, E->rho + R.goff, (cufftComplex *)(E->rhohat + R.khoff)));

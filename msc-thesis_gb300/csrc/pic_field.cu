@@ -14,14 +14,13 @@
 
 namespace pic {
 
-// rho = (rho_fix - mean) * scale, sum(rho_fix) -> dev->q, and rho_fix
-// cleared for the next deposit as it is read.  The background is removed in
-// exact integer arithmetic before the single rounding to float, so small
-// perturbations of a large mean keep their relative precision.  Two cells
-// per thread per iteration (16-byte loads and stores of the density, 8-byte
-// stores of rho).
+// rho = (rho_fix - mean) * scale, sum(rho_fix) -> dev->q; rho_fix is cleared
+// by a memset after this kernel.  The background is removed in exact integer
+// arithmetic before the single rounding to float, so small perturbations of a
+// large mean keep their relative precision.  Two cells per thread per
+// iteration (16-byte loads, 8-byte stores; n is even).
 __global__ void __launch_bounds__(256)
-convert_kernel(unsigned long long *__restrict__ rho_fix, float *__restrict__ rho, long long n,
+convert_kernel(const unsigned long long *__restrict__ rho_fix, float *__restrict__ rho, long long n,
                long long mean_fix, float scale, DevState *dev)
 {
     __shared__ unsigned long long s_part[8];
@@ -30,14 +29,12 @@ convert_kernel(unsigned long long *__restrict__ rho_fix, float *__restrict__ rho
     const long long n2 = n >> 1;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
         const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(rho_fix)[i];
-        reinterpret_cast<ulonglong2 *>(rho_fix)[i] = make_ulonglong2(0ull, 0ull);
         qs += v.x + v.y;
         reinterpret_cast<float2 *>(rho)[i] =
             make_float2(fixed_to_float(v.x, mean_fix, scale), fixed_to_float(v.y, mean_fix, scale));
     }
     if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long v = rho_fix[n - 1];
-        rho_fix[n - 1] = 0ull;
         qs += v;
         rho[n - 1] = fixed_to_float(v, mean_fix, scale);
     }
@@ -108,6 +105,7 @@ pic_status launch_convert(pic_handle *h)
     convert_kernel<<<grid_for((n + 1) / 2, 256), 256, 0, h->stream>>>(h->rho_fix, h->rho, n,
                                                                     h->mean_fix, scale, h->dev);
     PIC_CUDA(cudaGetLastError());
+    PIC_CUDA(cudaMemsetAsync(h->rho_fix, 0, sizeof(unsigned long long) * (size_t)n, h->stream));
     return PIC_OK;
 }
 
