@@ -189,11 +189,14 @@ __global__ void sort_anchor_kernel(SortArgs A, long long nchunks)
     A.anchor[b] = (t % A.ntx) | ((t / A.ntx) << 16);
 }
 
-// the scatter kernels use more than the default 48 KB of dynamic shared memory
+// the scatter kernels use more than the default 48 KB of dynamic shared
+// memory, and four of their blocks per SM need the largest carveout
 pic_status scatter_smem_attr(const void *kernel)
 {
     PIC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)SCATTER_SMEM));
+    PIC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
     return PIC_OK;
 }
 

@@ -203,8 +203,21 @@ __device__ __forceinline__ Run warp_run(int key)
     return r;
 }
 
-// Pass 1 of both kernels: keys of this thread's particles, counted in the
-// window or the table; a run the table had no room for gets FALLBACK_BIT.
+// Cells of this thread's particles (-1 past the end), loaded before the
+// window setup so that the two loads' latencies overlap.
+__device__ __forceinline__ void load_cells(const SortArgs &A, long long base, long long end,
+                                           int (&cells)[SORT_PER_THREAD])
+{
+#pragma unroll
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
+        cells[j] = (i < end) ? A.cin[i] : -1;
+    }
+}
+
+// Pass 1 of both kernels: keys of this thread's particles (`keys` holds
+// their cells from load_cells on entry), counted in the window or the
+// table; a run the table had no room for gets FALLBACK_BIT.
 __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, SortSmem &S,
                                            long long base, long long end, int k0, SortSizes Z,
                                            int (&keys)[SORT_PER_THREAD])
@@ -212,7 +225,7 @@ __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, S
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {
         const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
-        keys[j] = (i < end) ? particle_key(G, A.err, A.cin[i]) : -1;
+        keys[j] = (i < end) ? particle_key(G, A.err, keys[j]) : -1;
     }
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
@@ -241,10 +254,11 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
                                                 long long base, long long end)
 {
     const SortSizes Z = sort_sizes(A);
+    int keys[SORT_PER_THREAD];
+    load_cells(A, base, end, keys);
     const int k0 = window_start(A, G, base, end, Z.wk);
     init_smem(S, Z);
     __syncthreads();
-    int keys[SORT_PER_THREAD];
     count_keys(A, G, S, base, end, k0, Z, keys);
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
@@ -264,31 +278,41 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
         if (S.hcnt[r]) atomicAdd(A.count + S.hkey[r], S.hcnt[r]);
 }
 
-// Shared memory of a scatter block: the counting state, each key's first
-// slot in a block-local staging order, and the global destination of every
-// staged particle.  Once the destinations are known, the staging buffers
-// (three fields at a time) alias the counting state.
-struct ScatterSmem {
+// Shared memory of a scatter block: the counting state with each key's
+// first slot in a block-local staging order, and the global destination of
+// every staged particle.  Once the destinations are known, the staging
+// buffers (up to six fields at a time) take the counting state's place.
+// 56 KB: four blocks fill an SM's 228 KB with their 1 KB reserves.
+struct ScatterCount {
     SortSmem s;
     uint32_t lbase[SORT_KEYS];
     uint32_t hlbase[HASH_SLOTS];
-    uint32_t dst[SORT_CHUNK];
     uint32_t total;
 };
-static_assert(offsetof(ScatterSmem, dst) >= 3 * SORT_CHUNK * sizeof(uint32_t),
-              "staging buffers must fit in the counting state");
+constexpr int STAGE_FIELDS = 6;
+struct ScatterSmem {
+    union {
+        ScatterCount c;
+        uint32_t stage[STAGE_FIELDS * SORT_CHUNK];
+    };
+    uint32_t dst[SORT_CHUNK];
+};
+static_assert(sizeof(ScatterCount) <= STAGE_FIELDS * SORT_CHUNK * sizeof(uint32_t),
+              "the counting state must fit in the staging buffers");
 constexpr size_t SCATTER_SMEM = sizeof(ScatterSmem);
 
-// one staging phase: up to three 32-bit fields moved through shared memory
+// one staging phase: up to six 32-bit fields moved through shared memory
 // so that the global stores follow the destination order (consecutive
-// threads write consecutive slots of a key's slice)
+// threads write consecutive slots of a key's slice); `total` = particles
+// staged by the block
 template <int NF>
 __device__ __forceinline__ void stage_fields(ScatterSmem &S, long long base, long long end,
-                                             const int (&lpos)[SORT_PER_THREAD],
-                                             const uint32_t *const (&src)[3], uint32_t *const (&dst)[3])
+                                             const int (&lpos)[SORT_PER_THREAD], int total,
+                                             const uint32_t *const (&src)[NF], uint32_t *const (&dst)[NF])
 {
-    uint32_t *stage = reinterpret_cast<uint32_t *>(&S);
-    __syncthreads();  // previous phase has left the staging buffers
+    static_assert(NF <= STAGE_FIELDS, "staging buffers hold six fields");
+    uint32_t *stage = S.stage;
+    __syncthreads();  // the previous phase (or the counting state) has left the staging buffers
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {
         const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
@@ -298,7 +322,6 @@ __device__ __forceinline__ void stage_fields(ScatterSmem &S, long long base, lon
         }
     }
     __syncthreads();
-    const int total = (int)S.total;
     for (int t = threadIdx.x; t < total; t += SORT_THREADS) {
         const uint32_t d = S.dst[t];
         if (d == SORT_NO_SLOT) continue;
@@ -316,26 +339,28 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
                                                    ScatterSmem &S, long long base, long long end)
 {
     const SortSizes Z = sort_sizes(A);
-    const int k0 = window_start(A, G, base, end, Z.wk);
-    init_smem(S.s, Z);
-    if (threadIdx.x == 0) S.total = 0u;
-    __syncthreads();
     int keys[SORT_PER_THREAD];
-    count_keys(A, G, S.s, base, end, k0, Z, keys);
+    load_cells(A, base, end, keys);
+    const int k0 = window_start(A, G, base, end, Z.wk);
+    ScatterCount &C = S.c;
+    init_smem(C.s, Z);
+    if (threadIdx.x == 0) C.total = 0u;
+    __syncthreads();
+    count_keys(A, G, C.s, base, end, k0, Z, keys);
     __syncthreads();
     // reserve each distinct key's slice of the output and of the staging order
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
-        const uint32_t v = S.s.cnt[r];
+        const uint32_t v = C.s.cnt[r];
         const bool use = v && k0 + r < A.nkeys;
-        S.s.base[r] = use ? atomicAdd(A.cursor + k0 + r, v) : 0u;
-        S.lbase[r] = use ? atomicAdd(&S.total, v) : 0u;
-        S.s.cnt[r] = 0u;
+        C.s.base[r] = use ? atomicAdd(A.cursor + k0 + r, v) : 0u;
+        C.lbase[r] = use ? atomicAdd(&C.total, v) : 0u;
+        C.s.cnt[r] = 0u;
     }
     for (int r = threadIdx.x; r < (1 << Z.hb); r += SORT_THREADS) {
-        const uint32_t v = S.s.hcnt[r];
-        S.s.hbase[r] = v ? atomicAdd(A.cursor + S.s.hkey[r], v) : 0u;
-        S.hlbase[r] = v ? atomicAdd(&S.total, v) : 0u;
-        S.s.hcnt[r] = 0u;
+        const uint32_t v = C.s.hcnt[r];
+        C.s.hbase[r] = v ? atomicAdd(A.cursor + C.s.hkey[r], v) : 0u;
+        C.hlbase[r] = v ? atomicAdd(&C.total, v) : 0u;
+        C.s.hcnt[r] = 0u;
     }
     __syncthreads();
     // destination and staging slot of every particle: one reservation per run
@@ -347,17 +372,17 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
         if (R.head && key >= 0) {
             if (key & FALLBACK_BIT) {
                 d = atomicAdd(A.cursor + (key & ~FALLBACK_BIT), (uint32_t)R.len);
-                l = atomicAdd(&S.total, (uint32_t)R.len);
+                l = atomicAdd(&C.total, (uint32_t)R.len);
             } else if ((unsigned)(key - k0) < (unsigned)Z.wk) {
                 const int r = key - k0;
-                const uint32_t o = atomicAdd(S.s.cnt + r, (uint32_t)R.len);
-                d = S.s.base[r] + o;
-                l = S.lbase[r] + o;
+                const uint32_t o = atomicAdd(C.s.cnt + r, (uint32_t)R.len);
+                d = C.s.base[r] + o;
+                l = C.lbase[r] + o;
             } else {
-                const int slot = hash_find(S.s.hkey, key, Z.hb);  // counted in the table in pass 1
-                const uint32_t o = atomicAdd(S.s.hcnt + slot, (uint32_t)R.len);
-                d = S.s.hbase[slot] + o;
-                l = S.hlbase[slot] + o;
+                const int slot = hash_find(C.s.hkey, key, Z.hb);  // counted in the table in pass 1
+                const uint32_t o = atomicAdd(C.s.hcnt + slot, (uint32_t)R.len);
+                d = C.s.hbase[slot] + o;
+                l = C.hlbase[slot] + o;
             }
         }
         d = __shfl_sync(0xffffffffu, d, R.hidx) + (uint32_t)R.rank;
@@ -369,34 +394,30 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
         if (key >= 0) S.dst[l] = d;
         keys[j] = key >= 0 ? (int)l : -1;
     }
+    __syncthreads();  // the fallback runs' staging reservations are in
+    const int total = (int)C.total;  // read before the staging buffers overwrite it
     {
-        const uint32_t *const src[3] = {reinterpret_cast<const uint32_t *>(A.cin),
+        const uint32_t *const src[6] = {reinterpret_cast<const uint32_t *>(A.cin),
                                         reinterpret_cast<const uint32_t *>(A.oxin),
-                                        reinterpret_cast<const uint32_t *>(A.oyin)};
-        uint32_t *const dst[3] = {reinterpret_cast<uint32_t *>(A.cout),
-                                  reinterpret_cast<uint32_t *>(A.oxout),
-                                  reinterpret_cast<uint32_t *>(A.oyout)};
-        stage_fields<3>(S, base, end, keys, src, dst);
-    }
-    {
-        const uint32_t *const src[3] = {reinterpret_cast<const uint32_t *>(A.vxin),
+                                        reinterpret_cast<const uint32_t *>(A.oyin),
+                                        reinterpret_cast<const uint32_t *>(A.vxin),
                                         reinterpret_cast<const uint32_t *>(A.vyin), A.pidin};
-        uint32_t *const dst[3] = {reinterpret_cast<uint32_t *>(A.vxout),
+        uint32_t *const dst[6] = {reinterpret_cast<uint32_t *>(A.cout),
+                                  reinterpret_cast<uint32_t *>(A.oxout),
+                                  reinterpret_cast<uint32_t *>(A.oyout),
+                                  reinterpret_cast<uint32_t *>(A.vxout),
                                   reinterpret_cast<uint32_t *>(A.vyout), A.pidout};
-        stage_fields<3>(S, base, end, keys, src, dst);
+        stage_fields<6>(S, base, end, keys, total, src, dst);
     }
     if (A.vzin) {
-        const uint32_t *const src[3] = {reinterpret_cast<const uint32_t *>(A.vzin), nullptr, nullptr};
-        uint32_t *const dst[3] = {reinterpret_cast<uint32_t *>(A.vzout), nullptr, nullptr};
-        stage_fields<1>(S, base, end, keys, src, dst);
+        const uint32_t *const src[1] = {reinterpret_cast<const uint32_t *>(A.vzin)};
+        uint32_t *const dst[1] = {reinterpret_cast<uint32_t *>(A.vzout)};
+        stage_fields<1>(S, base, end, keys, total, src, dst);
     }
     if (A.xin[0]) {
-        const uint32_t *const src[3] = {A.xin[0], A.xin[1], A.xin[2]};
-        uint32_t *const dst[3] = {A.xout[0], A.xout[1], A.xout[2]};
-        stage_fields<3>(S, base, end, keys, src, dst);
-        const uint32_t *const src1[3] = {A.xin[3], nullptr, nullptr};
-        uint32_t *const dst1[3] = {A.xout[3], nullptr, nullptr};
-        stage_fields<1>(S, base, end, keys, src1, dst1);
+        const uint32_t *const src[4] = {A.xin[0], A.xin[1], A.xin[2], A.xin[3]};
+        uint32_t *const dst[4] = {A.xout[0], A.xout[1], A.xout[2], A.xout[3]};
+        stage_fields<4>(S, base, end, keys, total, src, dst);
     }
 }
 
