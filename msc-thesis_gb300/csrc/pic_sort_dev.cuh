@@ -186,6 +186,23 @@ struct Run {
     int rank;  // position of this lane in its run
 };
 
+// a Run in one word (head bit 0, head lane bits 1-5, length bits 6-11,
+// rank bits 12-16), kept from the count to the ranking phase
+__device__ __forceinline__ int pack_run(const Run &r)
+{
+    return (int)r.head | (r.hidx << 1) | (r.len << 6) | (r.rank << 12);
+}
+
+__device__ __forceinline__ Run unpack_run(int w)
+{
+    Run r;
+    r.head = w & 1;
+    r.hidx = (w >> 1) & 31;
+    r.len = (w >> 6) & 63;
+    r.rank = (w >> 12) & 31;
+    return r;
+}
+
 __device__ __forceinline__ Run warp_run(int key)
 {
     const unsigned full = 0xffffffffu;
@@ -217,10 +234,13 @@ __device__ __forceinline__ void load_cells(const SortArgs &A, long long base, lo
 
 // Pass 1 of both kernels: keys of this thread's particles (`keys` holds
 // their cells from load_cells on entry), counted in the window or the
-// table; a run the table had no room for gets FALLBACK_BIT.
+// table; a run the table had no room for gets FALLBACK_BIT (on all its
+// lanes, so the runs stay the same).  KEEP: each key's run, packed, to
+// `runs` for the ranking phase.
+template <bool KEEP>
 __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, SortSmem &S,
                                            long long base, long long end, int k0, SortSizes Z,
-                                           int (&keys)[SORT_PER_THREAD])
+                                           int (&keys)[SORT_PER_THREAD], int (&runs)[SORT_PER_THREAD])
 {
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {
@@ -244,8 +264,9 @@ __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, S
                     fb = 1;
             }
         }
-        fb = __shfl_sync(0xffffffffu, fb, R.hidx);
-        if (fb && key >= 0) keys[j] = key | FALLBACK_BIT;
+        const unsigned fbm = __ballot_sync(0xffffffffu, fb);  // heads whose run falls back
+        if (fbm && key >= 0 && ((fbm >> R.hidx) & 1u)) keys[j] = key | FALLBACK_BIT;
+        if (KEEP) runs[j] = pack_run(R);
     }
 }
 
@@ -259,7 +280,8 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
     const int k0 = window_start(A, G, base, end, Z.wk);
     init_smem(S, Z);
     __syncthreads();
-    count_keys(A, G, S, base, end, k0, Z, keys);
+    int unused[SORT_PER_THREAD];
+    count_keys<false>(A, G, S, base, end, k0, Z, keys, unused);
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
         // keys the block's table had no room for (rare): counted straight
@@ -346,7 +368,8 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
     init_smem(C.s, Z);
     if (threadIdx.x == 0) C.total = 0u;
     __syncthreads();
-    count_keys(A, G, C.s, base, end, k0, Z, keys);
+    int runs[SORT_PER_THREAD];
+    count_keys<true>(A, G, C.s, base, end, k0, Z, keys, runs);
     __syncthreads();
     // reserve each distinct key's slice of the output and of the staging order
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
@@ -367,7 +390,7 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
         const int key = keys[j];
-        const Run R = warp_run(key);
+        const Run R = unpack_run(runs[j]);
         uint32_t d = 0, l = 0;
         if (R.head && key >= 0) {
             if (key & FALLBACK_BIT) {
