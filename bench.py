@@ -433,7 +433,7 @@ def mcc_cross_sections(ntab=256, emin=0.01, emax=1000.0):
     return sel, sexc, sion
 
 
-def small_workload(P, kind, local):
+def small_workload(P, kind, local, chunk=0, tile=(0, 0)):
     """Handles of the other configurations, loaded and primed:
     c1    two-stream, 128^2, 100 ppc, beams +-0.2, vth 0.01, x-displacement
           1e-3 in k = 0.5, dt 0.1 (plasma units)
@@ -442,6 +442,7 @@ def small_workload(P, kind, local):
           3.2e21 m^-3 neutrals at 300 K, dt 1e-11 s
     dsmc  the mcc workload plus 50 hard-sphere neutrals per cell (6.6e-26 kg,
           d 3.6e-10 m), bimodal 300 K / 1000 K, Bird NTC every step
+    chunk, tile: push chunk and sort tile (0: the library's defaults).
     Returns (handle, particles pushed per step, cells, description, sort
     cadence)."""
     import numpy as np
@@ -452,7 +453,7 @@ def small_workload(P, kind, local):
         L = 4 * np.pi
         A = L * L
         cfg = P.config(nx, nx, L, L, 0.1, [P.species(n, -A / n, A / n, -1)], device=local,
-                       sort_every=20)
+                       sort_every=20, chunk=chunk, tile_w=tile[0], tile_h=tile[1])
         h = P.Handle(cfg)
         h.init_particles(0, P.init_spec(n, vth=(0.01, 0.01, 0.0), beam_v=0.2,
                                         pert_kind=P.PERT_XDISP, pert_amp=1e-3, pert_mx=1, seed=0))
@@ -472,7 +473,8 @@ def small_workload(P, kind, local):
     # a sort every 40 steps: 0.491 ms per step against 0.511 (20) and 0.546
     # (10) for mcc, 0.906 against 0.928 and 0.964 for dsmc (chunk 8192, the
     # default, within 1 % of 4096 and ahead of 16384)
-    cfg = P.config(nx, nx, L, L, 1e-11, sp, eps0=EPS0_SI, device=local, sort_every=40)
+    cfg = P.config(nx, nx, L, L, 1e-11, sp, eps0=EPS0_SI, device=local, sort_every=40,
+                   chunk=chunk, tile_w=tile[0], tile_h=tile[1])
     h = P.Handle(cfg)
     ve, vi = np.sqrt(2.0 * E_CH / M_E), np.sqrt(T_GAS_EV * E_CH / M_I)
     h.init_particles(0, P.init_spec(ne, vth=(ve, ve, ve), seed=5))
@@ -506,7 +508,8 @@ def bench_small(args):
     if rank != 0:
         return
     torch.cuda.set_device(local)
-    h, n, cells, desc, cadence = small_workload(P, args.workload, local)
+    h, n, cells, desc, cadence = small_workload(P, args.workload, local, args.chunk,
+                                                tuple(args.tile))
     stream = torch.cuda.ExternalStream(h.stream())
     h.step(args.warmup)
     h.synchronize()
@@ -533,6 +536,7 @@ def bench_small(args):
         "data": "synthetic",
         "config": {"workload": desc, "particles_pushed_per_step": n, "cells": cells,
                    "sort_every": cadence,
+                   "chunk": args.chunk or "default", "tile": list(args.tile) if args.tile[0] else "default",
                    "charge_exact": d.total_charge_fixed == d.expected_charge_fixed,
                    "error_flags": d.error_flags, "collision_counts": counts,
                    "peak_kind": peak_kind},

@@ -267,7 +267,7 @@ pic_status ens_layout(pic_ensemble *E)
         const double ppc = std::max(1.0, (double)D.capacity / (double)ncell);
         const int tcells = std::max(1, (int)std::lround(E->chunk / ppc));
         R.tw = pick_divisor(c.nx, std::min(16, tcells));
-        R.th = pick_divisor(c.ny, std::max(1, tcells / R.tw));
+        R.th = pick_tile_h(c.ny, tcells, R.tw);
         R.ntx = c.nx / R.tw;
         R.nty = c.ny / R.th;
         R.hx = R.hy = E->halo;

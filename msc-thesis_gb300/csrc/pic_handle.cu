@@ -69,6 +69,26 @@ int pick_divisor(int n, int target)
     return best;
 }
 
+// Tile height for a tile of about `tcells` cells and width tw: the divisor
+// of ny nearest to tcells / tw by ratio (so 6.4 gives 8, not 4: at 512^2 x
+// 64 particles per cell in 8192-particle chunks, 16 x 8 tiles took 0.470 ms
+// per step against 0.488 ms with 16 x 4).
+int pick_tile_h(int ny, int tcells, int tw)
+{
+    const double target = std::max(1.0, (double)tcells / (double)tw);
+    int best = 1;
+    double bd = 1e300;
+    for (int d = 1; d <= ny; ++d) {
+        if (ny % d) continue;
+        const double e = std::fabs(std::log((double)d / target));
+        if (e < bd - 1e-12) {
+            bd = e;
+            best = d;
+        }
+    }
+    return best;
+}
+
 static void free_handle_buffers(pic_handle *h)
 {
     for (int s = 0; s < PIC_MAX_SPECIES; ++s) {
@@ -179,7 +199,7 @@ static pic_status setup_geometry(pic_handle *h)
     const double ppc = std::max(1.0, (double)maxcap / ((double)c.nx * c.ny));
     const int tcells = std::max(1, (int)std::lround(g.chunk / ppc));
     g.tw = c.tile_w ? c.tile_w : pick_divisor(c.nx, std::min(16, tcells));
-    g.th = c.tile_h ? c.tile_h : pick_divisor(c.ny, std::max(1, tcells / g.tw));
+    g.th = c.tile_h ? c.tile_h : pick_tile_h(c.ny, tcells, g.tw);
     g.ntx = c.nx / g.tw;
     g.nty = c.ny / g.th;
     auto window = [&] {

@@ -275,5 +275,6 @@ bool stage_fits(pic_handle *h, size_t bytes);
 pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly);
 pic_status lattice_dims_for(int nx, int ny, long long n, int *lx, int *ly);
 int pick_divisor(int n, int target);
+int pick_tile_h(int ny, int tcells, int tw);
 
 }  // namespace pic
