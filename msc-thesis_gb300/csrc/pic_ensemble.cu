@@ -195,7 +195,7 @@ pic_status ens_bad(const std::string &m)
 
 size_t window_smem(const EnsRun &R)
 {
-    return (size_t)(R.wcx + 1) * (R.wcy + 1) * 16 + 32;
+    return window_bytes(R.wcx, R.wcy) + 32;
 }
 
 void ens_free(pic_ensemble *E)
@@ -273,7 +273,7 @@ pic_status ens_layout(pic_ensemble *E)
         R.hx = R.hy = E->halo;
         R.wcx = 2 * R.tw + 2 * R.hx;
         R.wcy = R.th + 2 * R.hy;
-        if (window_smem(R) > 48 * 1024) return ens_bad("shared-memory window too large for a run");
+        if (window_smem(R) > WINDOW_SMEM_MAX) return ens_bad("shared-memory window too large for a run");
         R.cap4 = (D.capacity + 3) & ~3ll;
         R.poff = poff;
         R.ncp = (ncell + 3) & ~3ll;
@@ -353,7 +353,7 @@ void ens_windows(pic_ensemble *E, const pic_init_spec *specs)
         for (;;) {
             R.wcx = 2 * R.tw + 2 * R.hx;
             R.wcy = R.th + 2 * R.hy;
-            if (window_smem(R) <= 48 * 1024 || (R.hx <= E->halo && R.hy <= E->halo)) break;
+            if (window_smem(R) <= WINDOW_SMEM_TARGET || (R.hx <= E->halo && R.hy <= E->halo)) break;
             if (R.hx >= R.hy && R.hx > E->halo)
                 --R.hx;
             else
@@ -433,6 +433,9 @@ pic_status ens_launch_push(pic_ensemble *E, int src, int kind)
     dim3 grid((unsigned)E->npush), block(256);
     const size_t sm = E->push_smem;
     cudaStream_t st = E->stream;
+    PIC_TRY(allow_dynamic_smem((const void *)ens_push_kernel<true, true>, sm));
+    PIC_TRY(allow_dynamic_smem((const void *)ens_push_kernel<true, false>, sm));
+    PIC_TRY(allow_dynamic_smem((const void *)ens_push_kernel<false, true>, sm));
     if (kind == 0)
         ens_push_kernel<true, true><<<grid, block, sm, st>>>(A, E->push_blk, E->d_runs, E->anchor, 1.f, 1.f);
     else if (kind == 1)
@@ -596,7 +599,8 @@ pic_status pic_ensemble_create(const pic_config *runs, int nruns, pic_ensemble *
     *out = nullptr;
     if (!runs || nruns < 1) return ens_bad("need at least one run");
     const pic_config &c0 = runs[0];
-    if (c0.chunk < 0 || c0.chunk % 4 || c0.halo < 0 || c0.sort_every < 0 || c0.history < 0)
+    if (c0.chunk < 0 || c0.chunk % 4 || c0.chunk > MAX_CHUNK || c0.halo < 0 || c0.sort_every < 0 ||
+        c0.history < 0)
         return ens_bad("bad chunk, halo, sort_every or history in runs[0]");
     for (int r = 0; r < nruns; ++r) {
         const pic_config &c = runs[r];

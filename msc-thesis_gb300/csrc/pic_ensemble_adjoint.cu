@@ -559,6 +559,8 @@ pic_status ens_adjoint(pic_ensemble *E, const pic_init_spec *specs, long long ns
     auto kick = [&](bool unkick, float cscale, float dscale) -> pic_status {
         PIC_CUDA(cudaMemsetAsync(g, 0, sizeof(float) * 2 * (size_t)E->nnodes, st));
         set_arrays();
+        PIC_TRY(allow_dynamic_smem((const void *)ens_adj_kick_kernel<true>, E->push_smem));
+        PIC_TRY(allow_dynamic_smem((const void *)ens_adj_kick_kernel<false>, E->push_smem));
         if (unkick)
             ens_adj_kick_kernel<true><<<E->npush, 256, E->push_smem, st>>>(A, E->push_blk, E->d_runs,
                                                                        E->anchor, cscale, dscale);

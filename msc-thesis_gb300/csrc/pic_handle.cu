@@ -170,7 +170,8 @@ static pic_status validate(const pic_config *c, pic_handle *h)
         }
     }
     if (h->q_unit == 0.0) h->q_unit = 1.0;
-    if (c->chunk < 0 || (c->chunk % 4) != 0) return bad("chunk must be a multiple of 4");
+    if (c->chunk < 0 || (c->chunk % 4) != 0 || c->chunk > MAX_CHUNK)
+        return bad("chunk must be a multiple of 4 and at most 32768");
     if (c->sort_every < 0 || c->halo < 0 || c->history < 0) return bad("negative tuning value");
     if (c->tile_w < 0 || c->tile_h < 0 || (c->tile_w && c->nx % c->tile_w) ||
         (c->tile_h && c->ny % c->tile_h))
@@ -205,14 +206,14 @@ static pic_status setup_geometry(pic_handle *h)
     auto window = [&] {
         g.wcx = 2 * g.tw + 2 * g.halo;
         g.wcy = g.th + 2 * g.halo;
-        return (size_t)(g.wcx + 1) * (g.wcy + 1) * 16 + 32;
+        return window_bytes(g.wcx, g.wcy) + 32;
     };
     size_t smem = window();
-    while (!c.halo && smem > 48 * 1024 && g.halo > 1) {
+    while (!c.halo && smem > WINDOW_SMEM_TARGET && g.halo > 1) {
         --g.halo;
         smem = window();
     }
-    if (smem > 48 * 1024) {
+    if (smem > WINDOW_SMEM_MAX) {
         set_error("pic_create: shared-memory window too large; use smaller tiles or halo");
         return PIC_ERR_INVALID_ARG;
     }

@@ -74,6 +74,30 @@ __host__ __device__ __forceinline__ double u01d(uint32_t r)
     return ((double)r + 0.5) * (1.0 / 4294967296.0);
 }
 
+// Shared-memory window of a push block covering wcx x wcy cells: E (float2)
+// at its (wcx + 1)(wcy + 1) nodes, then the deposit area: five 32-bit
+// moment planes of its cells (count, sum fx, sum fy, and the low 16 and the
+// high bits of sum fx*fy), with room also for two float planes of its nodes
+// (the ensemble adjoint kick's scatter sums); a multiple of 16 bytes.
+__host__ __device__ __forceinline__ size_t window_dep_words(int wcx, int wcy)
+{
+    const size_t nw = (size_t)(wcx + 1) * (wcy + 1), nc = (size_t)wcx * wcy;
+    return 5 * nc > 2 * nw ? 5 * nc : 2 * nw;
+}
+
+__host__ __device__ __forceinline__ size_t window_bytes(int wcx, int wcy)
+{
+    return ((size_t)(wcx + 1) * (wcy + 1) * 8 + window_dep_words(wcx, wcy) * 4 + 15) & ~(size_t)15;
+}
+
+// Largest push chunk: keeps every per-cell moment sum of a block below 2^31.
+constexpr int MAX_CHUNK = 32768;
+// Push windows: halos shrink until a block's shared memory fits four blocks
+// per SM (WINDOW_SMEM_TARGET); a window above WINDOW_SMEM_MAX even with
+// 1-cell halos is refused (smaller tiles).
+constexpr size_t WINDOW_SMEM_TARGET = 56 * 1024;
+constexpr size_t WINDOW_SMEM_MAX = 112 * 1024;
+
 // Philox stream identifiers (counter word 3)
 enum : uint32_t {
     STREAM_INIT = 0x696e6974u,   // "init"
@@ -204,6 +228,8 @@ namespace pic {
 pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale);
 size_t push_bulk_smem(const Geometry &g);
 size_t push_ws_smem(const Geometry &g);
+// lets `kernel` take `bytes` of dynamic shared memory (above the default 48 KB)
+pic_status allow_dynamic_smem(const void *kernel, size_t bytes);
 pic_status launch_deposit(pic_handle *h, int s);
 // pic_field.cu
 pic_status launch_convert(pic_handle *h);

@@ -39,7 +39,7 @@ namespace pic {
 // !MOVE: the deposit of the particles where they are (after an import, a
 // sort or a state load), through the same shared-memory windows.
 template <bool GATHER, bool DEPOSIT, bool AGG, bool MOVE = true>
-__global__ void __launch_bounds__(256) push_kernel(PushArgs A)
+__global__ void __launch_bounds__(256, 4) push_kernel(PushArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const long long n = *A.d_n;
@@ -111,9 +111,9 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 
 // shared memory of the bulk-copy variant: the window, the diagnostics, the
 // stage barriers, then the stage ring (16-byte aligned)
-__host__ __device__ __forceinline__ size_t tma_ring_offset(int nw)
+__host__ __device__ __forceinline__ size_t tma_ring_offset(size_t wbytes)
 {
-    return (((size_t)nw * 16 + 32 + PIPE_STAGES * 8) + 127) & ~(size_t)127;
+    return ((wbytes + 32 + PIPE_STAGES * 8) + 127) & ~(size_t)127;
 }
 
 template <bool GATHER, bool DEPOSIT>
@@ -126,9 +126,10 @@ __global__ void __launch_bounds__(256) push_kernel_bulk(PushArgs A)
     const long long n4 = (n + 3) & ~3ll;
     const long long end = min(base + (long long)A.chunk, n4);
     const Window W = setup_window(A.geo, smem, A.anchor[blockIdx.x]);
-    double *sAcc = reinterpret_cast<double *>(smem + (size_t)W.nw * 16);
-    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + (size_t)W.nw * 16 + 32);
-    unsigned char *ring = smem + tma_ring_offset(W.nw);
+    const size_t wb = window_bytes(A.geo.wcx, A.geo.wcy);
+    double *sAcc = reinterpret_cast<double *>(smem + wb);
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + wb + 32);
+    unsigned char *ring = smem + tma_ring_offset(wb);
     const int nstages = (int)((end - base + STAGE_PARTICLES - 1) / STAGE_PARTICLES);
     const size_t field_bytes = (size_t)STAGE_PARTICLES * 4;
     const size_t stage_bytes = 5 * field_bytes;
@@ -229,9 +230,9 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
 }
 
 // the window, the diagnostics, full and empty barriers, then the ring
-__host__ __device__ __forceinline__ size_t ws_ring_offset(int nw)
+__host__ __device__ __forceinline__ size_t ws_ring_offset(size_t wbytes)
 {
-    return (((size_t)nw * 16 + 32 + 2 * WS_STAGES * 8) + 127) & ~(size_t)127;
+    return ((wbytes + 32 + 2 * WS_STAGES * 8) + 127) & ~(size_t)127;
 }
 
 template <bool GATHER, bool DEPOSIT>
@@ -244,10 +245,11 @@ __global__ void __launch_bounds__(WS_THREADS) push_kernel_ws(PushArgs A)
     const long long n4 = (n + 3) & ~3ll;
     const long long end = min(base + (long long)A.chunk, n4);
     const Window W = setup_window(A.geo, smem, A.anchor[blockIdx.x]);
-    double *sAcc = reinterpret_cast<double *>(smem + (size_t)W.nw * 16);
-    unsigned long long *full = reinterpret_cast<unsigned long long *>(smem + (size_t)W.nw * 16 + 32);
+    const size_t wb = window_bytes(A.geo.wcx, A.geo.wcy);
+    double *sAcc = reinterpret_cast<double *>(smem + wb);
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(smem + wb + 32);
     unsigned long long *empty = full + WS_STAGES;
-    unsigned char *ring = smem + ws_ring_offset(W.nw);
+    unsigned char *ring = smem + ws_ring_offset(wb);
     const int nstages = (int)((end - base + WS_STAGE - 1) / WS_STAGE);
     constexpr size_t field_bytes = (size_t)WS_STAGE * 4;
     constexpr size_t stage_bytes = 5 * field_bytes;
@@ -332,8 +334,7 @@ __global__ void __launch_bounds__(WS_THREADS) push_kernel_ws(PushArgs A)
 
 size_t push_ws_smem(const Geometry &g)
 {
-    const int nw = (g.wcx + 1) * (g.wcy + 1);
-    return ws_ring_offset(nw) + (size_t)WS_STAGES * 5 * WS_STAGE * 4;
+    return ws_ring_offset(window_bytes(g.wcx, g.wcy)) + (size_t)WS_STAGES * 5 * WS_STAGE * 4;
 }
 
 // Deposit-only pass (after a sort or an import, before the first step):
@@ -371,13 +372,21 @@ __global__ void fixed_to_double_kernel(const unsigned long long *__restrict__ sr
 
 static size_t push_smem(const Geometry &g)
 {
-    return (size_t)(g.wcx + 1) * (g.wcy + 1) * 16 + 32;
+    return window_bytes(g.wcx, g.wcy) + 32;
+}
+
+// set on every launch: the attribute belongs to the current device, and a
+// process may drive several
+pic_status allow_dynamic_smem(const void *kernel, size_t bytes)
+{
+    if (bytes > 48 * 1024)
+        PIC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return PIC_OK;
 }
 
 size_t push_bulk_smem(const Geometry &g)
 {
-    const int nw = (g.wcx + 1) * (g.wcy + 1);
-    return tma_ring_offset(nw) + (size_t)PIPE_STAGES * 5 * STAGE_PARTICLES * 4;
+    return tma_ring_offset(window_bytes(g.wcx, g.wcy)) + (size_t)PIPE_STAGES * 5 * STAGE_PARTICLES * 4;
 }
 
 // set on every launch: the attribute belongs to the current device, and a
@@ -488,24 +497,34 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
         // warp-summed deposit groups: measured 5% slower at 2048^2 x 32 ppc
         // (1.144 vs 1.085 ms), so opt-in
         const size_t sm = push_smem(g);
-        if (charged && dep)
+        if (charged && dep) {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<true, true, true>, sm));
             push_kernel<true, true, true><<<grid, block, sm, h->stream>>>(A);
-        else if (charged)
+        } else if (charged) {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<true, false, false>, sm));
             push_kernel<true, false, false><<<grid, block, sm, h->stream>>>(A);
-        else if (dep)
+        } else if (dep) {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<false, true, true>, sm));
             push_kernel<false, true, true><<<grid, block, sm, h->stream>>>(A);
-        else
+        } else {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<false, false, false>, sm));
             push_kernel<false, false, false><<<grid, block, sm, h->stream>>>(A);
+        }
     } else {
         const size_t sm = push_smem(g);
-        if (charged && dep)
+        if (charged && dep) {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<true, true, false>, sm));
             push_kernel<true, true, false><<<grid, block, sm, h->stream>>>(A);
-        else if (charged)
+        } else if (charged) {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<true, false, false>, sm));
             push_kernel<true, false, false><<<grid, block, sm, h->stream>>>(A);
-        else if (dep)
+        } else if (dep) {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<false, true, false>, sm));
             push_kernel<false, true, false><<<grid, block, sm, h->stream>>>(A);
-        else
+        } else {
+            PIC_TRY(allow_dynamic_smem((const void *)push_kernel<false, false, false>, sm));
             push_kernel<false, false, false><<<grid, block, sm, h->stream>>>(A);
+        }
     }
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
@@ -520,6 +539,7 @@ pic_status launch_deposit(pic_handle *h, int s)
     const pic_species_desc &D = h->cfg.species[s];
     if (D.q_int == 0 || B.cap == 0 || B.nchunks == 0) return PIC_OK;
     const PushArgs A = push_args(h, s, 0, 0.f);
+    PIC_TRY(allow_dynamic_smem((const void *)push_kernel<false, true, false, false>, push_smem(h->g)));
     push_kernel<false, true, false, false><<<(unsigned)B.nchunks, 256, push_smem(h->g), h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;

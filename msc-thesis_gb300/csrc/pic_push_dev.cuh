@@ -36,12 +36,6 @@ __device__ __forceinline__ void deposit_global(unsigned long long *rho, int nx, 
     atomicAdd(rho + (size_t)cy1 * nx + cx1, W.w11 * q);
 }
 
-__device__ __forceinline__ void smem_add(unsigned *lo, unsigned *hi, int i, unsigned long long w)
-{
-    atomicAdd(lo + i, (unsigned)(w & 0xFFFFull));
-    atomicAdd(hi + i, (unsigned)(w >> 16));
-}
-
 // Per-run part of a push pass: the grid, its field and density, the
 // diagnostics, the tile window and the step coefficients.
 struct PushGeo {
@@ -79,12 +73,14 @@ struct PushArgs {
     PushGeo geo;
 };
 
-// Shared-memory window of a push block: E (float2) and the split deposit
-// accumulators, anchored at the tile of the block's first particle.
+// Shared-memory window of a push block (layout: window_bytes), anchored at
+// the tile of the block's first particle.  The deposit keeps per-cell CIC
+// moments in sM (plane k at sM + k nc); sLo and sHi are the same area seen
+// as two node planes by the ensemble adjoint kick.
 struct Window {
     float2 *sE;
-    unsigned *sLo, *sHi;
-    int wx0, wy0, nwx, nw;
+    unsigned *sLo, *sHi, *sM;
+    int wx0, wy0, nwx, nw, nc;
     bool on;
 };
 
@@ -96,6 +92,8 @@ __device__ __forceinline__ Window setup_window(const PushGeo &A, unsigned char *
     W.sE = reinterpret_cast<float2 *>(smem);
     W.sLo = reinterpret_cast<unsigned *>(smem + (size_t)W.nw * sizeof(float2));
     W.sHi = W.sLo + W.nw;
+    W.sM = W.sLo;
+    W.nc = A.wcx * A.wcy;
     W.on = anc >= 0;
     W.wx0 = W.wy0 = 0;
     if (W.on) {
@@ -145,34 +143,37 @@ template <bool GATHER, bool DEPOSIT>
 __device__ __forceinline__ void load_window(const PushGeo &A, const Window &W)
 {
     if (!W.on) return;
-    WindowWalk w(W);
-    for (int i = threadIdx.x; i < W.nw; i += blockDim.x, w.next(W)) {
-        if (GATHER) {
+    if (GATHER) {
+        WindowWalk w(W);
+        for (int i = threadIdx.x; i < W.nw; i += blockDim.x, w.next(W)) {
             const size_t g = w.node(W, A.nx, A.ny);
             W.sE[i] = make_float2(A.ex[g], A.ey[g]);
         }
-        if (DEPOSIT) {
-            W.sLo[i] = 0u;
-            W.sHi[i] = 0u;
-        }
     }
+    if (DEPOSIT)
+        for (int i = threadIdx.x; i < 5 * W.nc; i += blockDim.x) W.sM[i] = 0u;
 }
 
-// one group of particles in one cell: window or global
+// One group of `cnt` particles in one cell with sums fx, fy, fx*fy: its
+// moments added to the window's cell (five shared atomics; the node weights
+// are linear in them and are formed at the flush), or its node weights
+// straight to the grid outside the window.
 __device__ __forceinline__ void deposit_group(const PushGeo &A, const Window &W, int cx, int cy,
-                                              const Cic4 &C)
+                                              unsigned cnt, unsigned sfx, unsigned sfy,
+                                              unsigned long long sxy)
 {
     int dxl = cx - W.wx0, dyl = cy - W.wy0;
     if (dxl < 0) dxl += A.nx;
     if (dyl < 0) dyl += A.ny;
     if (W.on && dxl < A.wcx && dyl < A.wcy) {
-        const int i = dyl * W.nwx + dxl;
-        smem_add(W.sLo, W.sHi, i, C.w00);
-        smem_add(W.sLo, W.sHi, i + 1, C.w10);
-        smem_add(W.sLo, W.sHi, i + W.nwx, C.w01);
-        smem_add(W.sLo, W.sHi, i + W.nwx + 1, C.w11);
+        unsigned *m = W.sM + dyl * A.wcx + dxl;
+        atomicAdd(m, cnt);
+        atomicAdd(m + W.nc, sfx);
+        atomicAdd(m + 2 * W.nc, sfy);
+        atomicAdd(m + 3 * W.nc, (unsigned)(sxy & 0xFFFFull));
+        atomicAdd(m + 4 * W.nc, (unsigned)(sxy >> 16));
     } else {
-        deposit_global(A.rho, A.nx, A.ny, cx, cy, C, A.qmul);
+        deposit_global(A.rho, A.nx, A.ny, cx, cy, cic_weights(cnt, sfx, sfy, sxy), A.qmul);
     }
 }
 
@@ -312,15 +313,15 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
                 gfy += fy;
                 gxy += fxy;
             } else {
-                deposit_group(A, W, cx, cy, cic_weights(1u, fx, fy, fxy));
+                deposit_group(A, W, cx, cy, 1u, fx, fy, fxy);
             }
         }
     }
     if (DEPOSIT && AGG) {
         if (warp_group_sum(gcnt ? gkey : -1, gcnt, gfx, gfy, gxy) && gcnt)
-            deposit_group(A, W, gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+            deposit_group(A, W, gcx, gcy, gcnt, gfx, gfy, gxy);
     } else if (DEPOSIT && gcnt) {
-        deposit_group(A, W, gcx, gcy, cic_weights(gcnt, gfx, gfy, gxy));
+        deposit_group(A, W, gcx, gcy, gcnt, gfx, gfy, gxy);
     }
 }
 
@@ -368,9 +369,31 @@ __device__ __forceinline__ void finish_block(const PushGeo &A, const Window &W, 
         if (any_bad) atomicOr(&A.dev->err, (unsigned)PIC_DEVERR_NAN);
     }
     if (DEPOSIT && W.on) {
+        // node (a, b) takes w00 of cell (a, b), w10 of (a-1, b), w01 of
+        // (a, b-1) and w11 of (a-1, b-1), those inside the window
+        const int wcx = A.wcx, wcy = A.wcy, nc = W.nc;
+        const unsigned *m = W.sM;
+        auto sxy = [&](int l) {
+            return ((unsigned long long)m[l + 4 * nc] << 16) + m[l + 3 * nc];
+        };
         WindowWalk w(W);
         for (int i = threadIdx.x; i < W.nw; i += blockDim.x, w.next(W)) {
-            const unsigned long long v = ((unsigned long long)W.sHi[i] << 16) + W.sLo[i];
+            const int a = w.a, b = w.b;
+            unsigned long long v = 0ull;
+            if (a < wcx && b < wcy) {
+                const int l = b * wcx + a;
+                v += ((unsigned long long)m[l] << 32) -
+                     (((unsigned long long)m[l + nc] + m[l + 2 * nc]) << 16) + sxy(l);
+            }
+            if (a > 0 && b < wcy) {
+                const int l = b * wcx + a - 1;
+                v += ((unsigned long long)m[l + nc] << 16) - sxy(l);
+            }
+            if (a < wcx && b > 0) {
+                const int l = (b - 1) * wcx + a;
+                v += ((unsigned long long)m[l + 2 * nc] << 16) - sxy(l);
+            }
+            if (a > 0 && b > 0) v += sxy((b - 1) * wcx + a - 1);
             if (v) atomicAdd(A.rho + w.node(W, A.nx, A.ny), v * A.qmul);
         }
     }
@@ -387,7 +410,7 @@ __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, 
                                            long long base, long long end, int anc)
 {
     const Window W = setup_window(G, smem, anc);
-    double *sAcc = reinterpret_cast<double *>(smem + (size_t)W.nw * 16);
+    double *sAcc = reinterpret_cast<double *>(smem + window_bytes(G.wcx, G.wcy));
     load_window<GATHER, DEPOSIT>(G, W);
     if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
     __syncthreads();
