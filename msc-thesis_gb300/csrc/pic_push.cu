@@ -24,11 +24,15 @@
 // the total charge is exact.  Each thread owns four consecutive particles of
 // the sorted array (one 128-bit load per field); those that land in the same
 // cell are combined in registers (the four weights of a group follow from the
-// group's count and sums of fx, fy and fx*fy) before one set of atomics.  In
-// shared memory every node keeps two 32-bit accumulators, the low 16 bits and
-// the rest of its unsigned weight, so the hot atomics are native 32-bit adds;
-// the charge sign is applied once per node when the window is flushed with a
-// 64-bit atomic to the global density.
+// group's count and sums of fx, fy and fx*fy) before one set of atomics.
+// Because the weights are linear in those moments, the shared-memory window
+// keeps per cell five 32-bit sums (count, sum fx, sum fy, and the low 16 and
+// the high bits of sum fx*fy): five native 32-bit atomics per group instead
+// of two per node (eight), on the shared-memory pipe that limits this
+// kernel.  At the end of the block each window node forms its weight from
+// the moments of its four cells and the charge sign is applied once per
+// node in a 64-bit atomic to the global density.  Per block and cell the
+// sums stay below 2^31 for chunks of at most 32768 particles.
 #include <cuda_runtime.h>
 
 #include "pic_push_dev.cuh"
