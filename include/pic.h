@@ -119,9 +119,11 @@ typedef struct pic_config {
     pic_species_desc species[PIC_MAX_SPECIES];
     int sort_every;      /* steps between counting sorts (0: 20)              */
     int tile_w, tile_h;  /* sort tile in cells (0: chosen from the density)   */
-    int chunk;           /* particles per push block, multiple of 4 (0: 8192) */
+    int chunk;           /* particles per push block, multiple of 4, at most
+                            32768 (0: 8192)                                   */
     int halo;            /* shared-memory window halo in cells (0: 4, or less
-                            where the window would exceed 48 KB)             */
+                            where the window would exceed 56 KB; windows over
+                            112 KB are refused)                               */
     int history;         /* diagnostic history length in steps (0: 4096)      */
     int device;          /* CUDA device ordinal                               */
     int push_variant;    /* 0: auto (1), 1: direct 128-bit loads, 2: bulk-copy

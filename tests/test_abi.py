@@ -55,6 +55,11 @@ def test_config_validation_is_host_side():
     with pytest.raises(P.PicError) as e:
         P.Handle(bad)
     assert e.value.status == 1
+    # push chunks above 32768 particles could overflow the window's 32-bit cell moments
+    bad = P.config(64, 64, 1.0, 1.0, 0.1, [P.species(100, -1.0, 1.0, -1)], chunk=32772)
+    with pytest.raises(P.PicError) as e:
+        P.Handle(bad)
+    assert e.value.status == 1
 
 
 def test_compat_params_validation_is_host_side():
