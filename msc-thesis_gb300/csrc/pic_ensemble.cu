@@ -335,7 +335,7 @@ pic_status ens_layout(pic_ensemble *E)
 // Window halos from the fastest particles of each run's load: the halo
 // along an axis covers half the drift of a sort period (the mean
 // displacement at which a particle is pushed), at least the configured halo,
-// as far as the 48 KB shared-memory window allows.
+// as far as a window of WINDOW_SMEM_TARGET bytes allows.
 void ens_windows(pic_ensemble *E, const pic_init_spec *specs)
 {
     E->push_smem = 0;
