@@ -90,7 +90,8 @@ __host__ __device__ __forceinline__ size_t window_bytes(int wcx, int wcy)
     return ((size_t)(wcx + 1) * (wcy + 1) * 8 + window_dep_words(wcx, wcy) * 4 + 15) & ~(size_t)15;
 }
 
-// Largest push chunk: keeps every per-cell moment sum of a block below 2^31.
+// Largest push chunk: every per-cell moment sum of a block stays at most 2^31,
+// inside its unsigned 32-bit word.
 constexpr int MAX_CHUNK = 32768;
 // Push windows: halos shrink until a block's shared memory fits four blocks
 // per SM (WINDOW_SMEM_TARGET); a window above WINDOW_SMEM_MAX even with

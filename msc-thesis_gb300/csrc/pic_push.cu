@@ -32,7 +32,7 @@
 // kernel.  At the end of the block each window node forms its weight from
 // the moments of its four cells and the charge sign is applied once per
 // node in a 64-bit atomic to the global density.  Per block and cell the
-// sums stay below 2^31 for chunks of at most 32768 particles.
+// sums stay at most 2^31 for chunks of at most 32768 particles.
 #include <cuda_runtime.h>
 
 #include "pic_push_dev.cuh"
