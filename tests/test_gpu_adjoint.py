@@ -43,13 +43,15 @@ def test_gpu_adjoint_matches_fp64_adjoint(setup, nsteps):
         r, gx, gy, gvx, gvy = h.adjoint(nsteps, every=8)
     J, ox, oy, ovx, ovy = O.adjoint(ocfg, s0["x"], s0["y"], s0["vx"], s0["vy"], q, m, nsteps)
     print(nsteps, "J", r.J, J)
-    assert r.J == pytest.approx(J, rel=1e-4)
+    assert r.J == pytest.approx(J, rel=1e-5)
     errs = [rel_norm(a, b) for a, b in ((gx, ox), (gy, oy), (gvx, ovx), (gvy, ovy))]
     print("gradient rel norm errors", errs)
-    assert max(errs) < (2e-3 if nsteps <= 10 else 2e-2)
+    # per-particle gradients carry the FP32 trajectory's node crossings
+    # (measured 1e-5 after 10 steps, 1e-4 after 50)
+    assert max(errs) < (1e-4 if nsteps <= 10 else 1e-3)
     drift_gpu, drift_orc = np.sum(sign * gvx), np.sum(sign * ovx)
     print("d/d(drift)", drift_gpu, drift_orc)
-    assert drift_gpu == pytest.approx(drift_orc, rel=1e-3)
+    assert drift_gpu == pytest.approx(drift_orc, rel=1e-4)
 
 
 def test_checkpoint_interval_does_not_change_the_gradient(setup):
@@ -110,12 +112,43 @@ def test_load_parameter_gradients(setup):
     sign = np.where(i % 2 == 0, 1.0, -1.0)
     damp, dbeam = np.sum(ox * dxdA), np.sum(sign * ovx)
     print("J", r.J, J, "damp", r.dJ_damp, damp, "dbeam", r.dJ_dbeam_v, dbeam)
-    assert r.J == pytest.approx(J, rel=1e-4)
-    assert r.dJ_damp == pytest.approx(damp, rel=2e-3)
-    assert r.dJ_dbeam_v == pytest.approx(dbeam, rel=2e-3)
+    assert r.J == pytest.approx(J, rel=1e-5)
+    assert r.dJ_damp == pytest.approx(damp, rel=1e-4)
+    assert r.dJ_dbeam_v == pytest.approx(dbeam, rel=1e-4)
     # the contraction done on the device equals the one done here on its own arrays
     assert r.dJ_damp == pytest.approx(np.sum(gx * dxdA), rel=1e-9, abs=1e-12)
     assert r.dJ_dbeam_v == pytest.approx(np.sum(sign * gvx), rel=1e-9, abs=1e-12)
+
+
+@pytest.mark.parametrize("dt,nsteps,every", [(0.1, 50, 10), (0.01, 500, 50)])
+def test_load_parameter_gradients_match_central_differences(dt, nsteps, every):
+    """dJ/d(beam_v) and dJ/d(pert_amp) of the GPU adjoint (contracted on the
+    device from the load) against central differences (eps 1e-8) of the FP64
+    forward map of the same load family, within 1e-4; the FP64 adjoint of
+    the family is checked against the same differences.  The 500-step case
+    keeps a checkpoint every 50 steps, at dt = 0.01: 500 steps of dt = 0.1
+    end past the saturation of the two-stream modes, where the map is
+    chaotic and neither differences nor an FP32 trajectory follow it."""
+    from adjoint_util import central_differences, family_from_device, fp64_adjoint, rel
+    n = NX * NX * PPC
+    v0, amp = 0.2, 1e-3
+    cfg, q, m = normalized_electrons(NX, NX, L, L, n, dt)
+    spec = P.init_spec(n, layout=P.LOAD_LATTICE, vth=(0.01, 0.01, 0.0), beam_v=v0,
+                       pert_kind=P.PERT_XDISP, pert_amp=amp, pert_mx=1, seed=11)
+    with P.Handle(cfg) as h:
+        h.init_particles(0, spec)
+        r = h.adjoint(nsteps, every=every, spec=spec)[0]
+    fam = family_from_device(P, cfg, n, 11, P.LOAD_LATTICE)
+    ocfg = O.PhysCfg(NX, NX, L, L, dt, 1.0, 1)
+    J, (adj_v, adj_a) = fp64_adjoint(ocfg, fam, q, m, nsteps, v0, amp)
+    fd_v, fd_a = central_differences(ocfg, fam, q, m, nsteps, v0, amp)
+    print(f"dt {dt}, {nsteps} steps: J gpu {r.J:.8e} fp64 {J:.8e}; dJ/dv0 gpu {r.dJ_dbeam_v:.8e} "
+          f"fp64 {adj_v:.8e} FD {fd_v:.8e} ({rel(r.dJ_dbeam_v, fd_v):.1e}); dJ/damp gpu "
+          f"{r.dJ_damp:.8e} fp64 {adj_a:.8e} FD {fd_a:.8e} ({rel(r.dJ_damp, fd_a):.1e})")
+    assert rel(adj_v, fd_v) < 1e-4 and rel(adj_a, fd_a) < 1e-4
+    assert rel(r.dJ_dbeam_v, fd_v) < 1e-4
+    assert rel(r.dJ_damp, fd_a) < 1e-4
+    assert r.J == pytest.approx(J, rel=1e-5)
 
 
 def test_torch_binding_gradients(setup):

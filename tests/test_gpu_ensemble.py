@@ -101,7 +101,7 @@ def test_ensemble_field_energy_matches_fp64_oracle():
         ref = st.run(nst, nthreads=0)
         rel = np.abs(fe_ens[r] - ref["fe"]) / ref["fe"].max()
         print(f"run {r}: field energy max rel error vs FP64 oracle {rel.max():.2e}")
-        assert rel.max() < 1e-4
+        assert rel.max() < 1e-5  # measured 8e-7 and 1.5e-6
 
 
 def test_ensemble_rejects_bad_configs():

@@ -29,7 +29,7 @@ def test_short_run_matches_fp64_oracle():
         fe = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
         rel = np.abs(fe - ref["fe"]) / ref["fe"].max()
         print("field energy max rel err", rel.max())
-        assert rel.max() < 2e-4
+        assert rel.max() < 1e-5
         ke = h.history(P.HIST_KINETIC, 0, nst)
         np.testing.assert_allclose(ke, ref["ke"], rtol=2e-4)
         a = h.get_particles()

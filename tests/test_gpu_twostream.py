@@ -76,11 +76,14 @@ def test_two_stream_128_matches_fp64_oracle_early_phase():
     ref = st.run(nst, nthreads=0)
     err_fe = np.max(np.abs(fe - ref["fe"]) / ref["fe"])
     err_ke = np.max(np.abs(ke - ref["ke"]) / ref["ke"])
-    print(f"field energy max rel err {err_fe:.2e}, kinetic {err_ke:.2e}")
-    assert err_fe < 1e-3
-    assert err_ke < 1e-5
-    np.testing.assert_allclose(rho, ref["rho"], atol=2e-3 * np.abs(ref["rho"]).max())
-    np.testing.assert_allclose(ex, ref["ex"], atol=2e-3 * np.abs(ref["ex"]).max())
+    err_rho = np.abs(rho - ref["rho"]).max() / np.abs(ref["rho"]).max()
+    err_ex = np.abs(ex - ref["ex"]).max() / np.abs(ref["ex"]).max()
+    print(f"field energy max rel err {err_fe:.2e}, kinetic {err_ke:.2e}, rho {err_rho:.2e}, "
+          f"Ex {err_ex:.2e}")
+    assert err_fe < 1e-5  # measured 7e-7
+    assert err_ke < 1e-7  # measured 1e-8
+    assert err_rho < 1e-4  # measured 7e-6
+    assert err_ex < 1e-4  # measured 2e-6
 
 
 def test_two_stream_128_full_run_conserves_energy_charge_momentum():
