@@ -8,7 +8,10 @@ a counting sort every `sort_every` steps): the large collisionless run,
 Maxwellian vth = 0.05 with a density perturbation of amplitude 0.01 in mode
 (1,1), dt = 0.05, plasma units (eps0 = 1, omega_pe = 1), L = 2048 * 0.05.
 Data are synthetic (seeded Philox init).  The particle arrays (2.7 GB per
-pass) are far larger than L2, so no flush is needed between steps.
+pass) are far larger than L2, so no flush is needed between steps.  The K
+timed steps hold whole sort periods (the cadence is the largest divisor of K
+not above the autotuned one; the untimed warm-up ends on a period boundary),
+so the rate is the steady state with the sort's cost amortised.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -145,8 +148,10 @@ def launches_for(k, since_sort, S, nspecies=1, per_sort=6):
     return sorts * per_sort * nspecies + k * (nspecies + 4), sorts, after
 
 
-def cpu_sample(nthreads):
-    """The reference's CPU step (oracle restatement, OpenMP) on a bounded
+def cpu_sample():
+    """The reference's CPU step (the oracle's operation-for-operation
+    restatement of thesisCode/collisionless/double/src/{grid,fourier,
+    particle}.cc, bit-identical to the compiled reference) on a bounded
     sample of the workload: 512 x 512 cells at 32 particles per cell."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
@@ -160,14 +165,22 @@ def cpu_sample(nthreads):
     return p, (x, y, vx, vy), n, f"512x512 cells, 32 ppc ({n} particles), reference conventions"
 
 
-def time_cpu(steps, nthreads):
+def time_cpu(nthreads, warmup, steps):
+    """particle-steps/s of the CPU step on the sample: `warmup` untimed steps,
+    then `steps` timed steps from the warmed state, on `nthreads` threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    p, st, n, desc = cpu_sample(nthreads)
+    if not os.path.exists(os.path.join(ROOT, "oracle", "build", "liboracle.so")):
+        O.build()
+    p, st, n, desc = cpu_sample()
+    if warmup:
+        w = O.compat_run(p, *st, warmup, nthreads=nthreads)
+        st = (w["x"], w["y"], w["vx"], w["vy"])
     t0 = time.perf_counter()
     O.compat_run(p, *st, steps, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    return n * steps / dt, desc, n
+    el = time.perf_counter() - t0
+    return n * steps / el, el, desc
 
 
 def fp64_check(P, cfg, spec, q, m, nsteps):
@@ -198,18 +211,8 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-
-    if not os.path.exists(os.path.join(ROOT, "oracle", "build", "liboracle.so")):
-        O.build()
     nthreads = os.cpu_count() or 1
-    p, st, n, desc = cpu_sample(nthreads)
-    O.compat_run(p, *st, max(1, args.warmup), nthreads=nthreads)
-    t0 = time.perf_counter()
-    O.compat_run(p, *st, args.steps, nthreads=nthreads)
-    el = time.perf_counter() - t0
-    v = n * args.steps / el
+    v, el, desc = time_cpu(nthreads, max(1, args.warmup), args.steps)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -623,13 +626,21 @@ def main():
         tuned = {"chunk": r.chunk, "tile": [r.tile_w, r.tile_h], "sort_every": r.sort_every,
                  "trial_ms_per_step": r.ms_per_step, "candidates": r.tried}
         SORT_EVERY = r.sort_every
+    # the timed steps hold whole sort periods: the cadence is the largest
+    # divisor of K not above the chosen one, and the warm-up is extended to
+    # end on a period boundary, so the K steps are K / S sorts and K steps
+    S = max(d for d in range(1, min(SORT_EVERY, args.steps) + 1) if args.steps % d == 0)
+    cfg.sort_every = S
+    SORT_EVERY = S
+    _, since = schedule(args.warmup, 0, S)
+    align = S - since if since < S else 0
     h = P.Handle(cfg)
     h.init_particles(0, spec)
     h.prime_leapfrog()
     stream = torch.cuda.ExternalStream(h.stream())
 
     # warm-up, then exactly K timed steps bracketed by barrier + synchronize
-    h.step(args.warmup)
+    h.step(args.warmup + align)
     h.synchronize()
     clocks = Clocks(local)
     clocks.start()
@@ -661,6 +672,13 @@ def main():
     h.synchronize()
     push_ms = p0.elapsed_time(p1) / reps
     h.poisson()
+    # then one periodic sort on its own (eager, same stream), for the breakdown
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    h.sort()
+    s1.record(stream)
+    h.synchronize()
+    sort_ms = s0.elapsed_time(s1)
     hbm, peak_kind = peaks()
     achieved = BYTES_PER_PARTICLE * N / (push_ms / 1000.0) / 1e9
     step_bytes = BYTES_PER_PARTICLE * N + BYTES_PER_CELL * NX * NY
@@ -690,15 +708,22 @@ def main():
     cpu = None
     fp64 = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        # the reference's step is serial: the baseline is one core; the same
+        # step on all host cores, timed as --impl reference times it, beside it
         nthreads = os.cpu_count() or 1
-        v, desc, _ = time_cpu(2, nthreads)
-        cpu = {"value": v, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
-               "sample": desc + ", 2 steps"}
+        v1, el1, desc = time_cpu(1, 1, 3)
+        vall, elall, _ = time_cpu(nthreads, args.warmup, args.steps)
+        cpu = {"value": v1, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": desc + ", 3 steps after 1 warm-up step",
+               "all_cores": {"value": vall, "cores": nthreads,
+                             "sample": desc + f", {args.steps} steps after {args.warmup} warm-up "
+                                              "steps (the --impl reference protocol)"},
+               "note": "the port is the oracle's bit-identical restatement of the reference's "
+                       "serial CPU step; the compiled reference itself is not on this host"}
         if args.nx == NX:
             fp64 = fp64_check(P, cfg, spec, -A / N, A / N, 10)
 
-    _, _, since_after_warmup = launches_for(args.warmup, 0, SORT_EVERY)
+    _, _, since_after_warmup = launches_for(args.warmup + align, 0, SORT_EVERY)
     launches, sorts_timed, _ = launches_for(args.steps, since_after_warmup, SORT_EVERY)
     if rank == 0:
         out = {
@@ -709,6 +734,8 @@ def main():
             "config": {"workload": f"landau-{NX}x{NY}-{PPC}ppc", "nx": NX, "ny": NY,
                        "particles": N, "dt": DT, "sort_every": SORT_EVERY,
                        "sorts_in_timed_steps": sorts_timed,
+                       "untimed_steps_before": args.warmup + align,
+                       "sort_ms": sort_ms,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (2.7 GB particle arrays per step)",
                        "hbm_frac_step": step_bytes * args.steps / (ms_max / 1000.0) / 1e9 / hbm,

@@ -47,7 +47,8 @@ typedef enum pic_status {
     PIC_ERR_CUFFT = 4,       /* a cuFFT call failed                        */
     PIC_ERR_OVERFLOW = 5,    /* capacity exceeded (particles, cells)       */
     PIC_ERR_NAN = 6,         /* non-finite particle state detected         */
-    PIC_ERR_TIMEOUT = 7,     /* a bounded device wait gave up              */
+    PIC_ERR_TIMEOUT = 7,     /* a bounded device wait gave up (no kernel of
+                                this library waits on another)             */
     PIC_ERR_STATE = 8,       /* call not valid in the handle's state       */
     PIC_ERR_NO_DEVICE = 9    /* no CUDA device visible                     */
 } pic_status;
@@ -126,12 +127,10 @@ typedef struct pic_config {
                             112 KB are refused)                               */
     int history;         /* diagnostic history length in steps (0: 4096)      */
     int device;          /* CUDA device ordinal                               */
-    int push_variant;    /* 0: auto (1), 1: direct 128-bit loads, 2: bulk-copy
-                            pipeline with block-wide stages, 3: direct loads
-                            with deposit groups summed across the warp,
-                            4: bulk-copy pipeline, one producer warp and
-                            consumer warps on mbarriers (2 and 4 need chunk
-                            a multiple of 1024)                               */
+    int push_variant;    /* 0: auto (1), 1: direct 128-bit loads, 3: direct
+                            loads with deposit groups summed across the warp
+                            (2 and 4, bulk-copy pipelines measured slower
+                            than 1, were removed and are refused)             */
 } pic_config;
 
 typedef struct pic_handle pic_handle;
@@ -300,9 +299,10 @@ pic_status pic_run_host(pic_handle *h, long long n, const double *x, const doubl
  * the file: set them on the loading handle.  No counterpart in the
  * reference (it keeps no state between runs). */
 pic_status pic_save(pic_handle *h, const char *path);
-/* Load a state file into a handle created with the same nx, ny, Lx, Ly and
- * species count (same flags and q_int), each species' capacity at least the
- * saved count; the field is recomputed from the loaded positions.  The
+/* Load a state file into a handle created with the same nx, ny, Lx, Ly, dt,
+ * eps0 and species (same count, flags, q_int, q and m), each species'
+ * capacity at least the saved count; the field is recomputed from the
+ * loaded positions.  The
  * whole file is read and checked first (cells on the grid or -1, offsets in
  * [0, 1), finite velocities, ids a permutation, no trailing bytes): a bad
  * file returns PIC_ERR_INVALID_ARG and leaves the handle unchanged. */
@@ -374,7 +374,8 @@ enum pic_device_errors {
     PIC_DEVERR_NAN = 1,       /* a particle had a non-finite velocity          */
     PIC_DEVERR_CAPACITY = 2,  /* a species ran out of capacity (ionisation)    */
     PIC_DEVERR_CELL = 4,      /* a cell index outside the grid was seen        */
-    PIC_DEVERR_TIMEOUT = 8,   /* a bounded device wait gave up                 */
+    PIC_DEVERR_TIMEOUT = 8,   /* a bounded device wait gave up (unused: no
+                                 kernel of this library waits on another)     */
     PIC_DEVERR_SORT = 16      /* a sort destination fell outside the slots
                                  (cell counts inconsistent with the particles;
                                  the particle was left unmoved)               */
@@ -468,8 +469,10 @@ pic_status pic_get_rho_fixed(pic_handle *h, int64_t *out);
  * into rho_dev (nx*ny doubles, row-major [iy][ix]), which is overwritten
  * with q_int * scale * (fixed-point density / 2^32).  Accumulates in an
  * int64 scratch grid that this call allocates on the device and frees.
- * stream may be NULL (legacy default stream).  Entries with cell < 0 are
- * skipped. */
+ * stream may be NULL (legacy default stream).  Entries with cell < 0 and
+ * cells off the grid are skipped without a report (the handle's kernels
+ * report off-grid cells as PIC_DEVERR_CELL).  Returns after the deposit has
+ * finished (it synchronises the stream). */
 pic_status pic_deposit_grid(int nx, int ny, long long n, const int32_t *cell_dev,
                             const float *ox_dev, const float *oy_dev, int q_int, double scale,
                             double *rho_dev, void *stream);
@@ -480,11 +483,15 @@ pic_status pic_deposit_grid(int nx, int ny, long long n, const int32_t *cell_dev
  * not pay cudaFree's device-wide synchronisation.  No counterpart in the
  * reference.  The int64 scratch grid is a static device array of
  * PIC_NOALLOC_MAX_CELLS cells (8 MiB held on every GPU that loads the
- * library); nx*ny above that is rejected with PIC_ERR_INVALID_ARG.  The call
- * only enqueues work on `stream` (NULL: legacy default stream) and returns.
+ * library); nx*ny above that is rejected with PIC_ERR_INVALID_ARG.  Unlike
+ * pic_deposit_grid the call only enqueues work on `stream` (NULL: legacy
+ * default stream) and returns: synchronise the stream before reading rho_dev
+ * or reusing the particle arrays; kernel faults surface at that sync.
  * All calls share the scratch grid: calls whose work overlaps on the GPU
- * race.  The first call on a device looks up the scratch address with that
- * device current; make it before any stream capture on that device. */
+ * race.  Every call looks up the scratch address on the current device; the
+ * first call on a device also loads the library's device code there, so make
+ * it before any stream capture on that device.  Cells off the grid are
+ * skipped without a report, as in pic_deposit_grid. */
 #define PIC_NOALLOC_MAX_CELLS (1 << 20)
 pic_status pic_deposit_grid_noalloc(int nx, int ny, long long n, const int32_t *cell_dev,
                                     const float *ox_dev, const float *oy_dev, int q_int,

@@ -173,6 +173,8 @@ static pic_status validate(const pic_config *c, pic_handle *h)
     if (c->chunk < 0 || (c->chunk % 4) != 0 || c->chunk > MAX_CHUNK)
         return bad("chunk must be a multiple of 4 and at most 32768");
     if (c->sort_every < 0 || c->halo < 0 || c->history < 0) return bad("negative tuning value");
+    if (c->push_variant != 0 && c->push_variant != 1 && c->push_variant != 3)
+        return bad("push_variant must be 0, 1 or 3");
     if (c->tile_w < 0 || c->tile_h < 0 || (c->tile_w && c->nx % c->tile_w) ||
         (c->tile_h && c->ny % c->tile_h))
         return bad("tile_w, tile_h must divide nx, ny");
@@ -217,18 +219,6 @@ static pic_status setup_geometry(pic_handle *h)
         set_error("pic_create: shared-memory window too large; use smaller tiles or halo");
         return PIC_ERR_INVALID_ARG;
     }
-    // the bulk-copy pipeline streams whole stages of 1024 particles
-    const bool bulk_ok = (g.chunk % 1024) == 0 && push_bulk_smem(g) <= 200 * 1024;
-    const bool ws_ok = (g.chunk % 1024) == 0 && push_ws_smem(g) <= 220 * 1024;
-    if (c.push_variant < 0 || c.push_variant > 4 || (c.push_variant == 2 && !bulk_ok) ||
-        (c.push_variant == 4 && !ws_ok)) {
-        set_error("pic_create: push_variant 2 and 4 need chunk a multiple of 1024 and a smaller window");
-        return PIC_ERR_INVALID_ARG;
-    }
-    // measured at 2048^2 x 32 ppc: the direct kernel (1.05 ms) beats the
-    // bulk-copy pipelines (block-wide stages 1.27 ms; producer and consumer
-    // warps on mbarriers 1.095 ms, 3 blocks per SM), so auto picks direct
-    h->use_bulk = (c.push_variant == 2);
     return PIC_OK;
 }
 

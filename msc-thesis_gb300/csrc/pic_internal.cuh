@@ -211,8 +211,6 @@ struct pic_handle {
     // collision operators
     pic::MccState mcc;
     pic::DsmcState dsmc;
-    // push kernel variant: bulk-copy pipeline (chunk a multiple of its stage)
-    bool use_bulk = false;
     // radix sort temporary storage of the import sort
     void *cub_temp = nullptr;
     size_t cub_temp_bytes = 0;
@@ -227,8 +225,6 @@ namespace pic {
 // ------------------------------------------------------------------ launchers
 // pic_push.cu
 pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_scale);
-size_t push_bulk_smem(const Geometry &g);
-size_t push_ws_smem(const Geometry &g);
 // lets `kernel` take `bytes` of dynamic shared memory (above the default 48 KB)
 pic_status allow_dynamic_smem(const void *kernel, size_t bytes);
 pic_status launch_deposit(pic_handle *h, int s);

@@ -14,25 +14,28 @@
 // The scratch array is shared by every call in the process: each call clears
 // the part it uses before depositing, and calls whose work overlaps on the GPU
 // (different streams, or different host threads) race on it and give wrong
-// results.  The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress, with that device current) and caches it; make that
-// first call before any stream capture on that device.
+// results.  Every call looks up the array's device address on the current
+// device (cudaGetSymbolAddress) instead of keeping it: a cudaDeviceReset or a
+// re-created primary context reloads the module at another address, and a
+// kept pointer would then be stale.  The first call on a device also loads
+// the module there; make it before any stream capture on that device.
+//
+// The call is asynchronous: it only enqueues work on the caller's stream.
+// Synchronise that stream before reading rho_dev or reusing the particle
+// arrays.  Entries with cell < 0 (empty slots) and cells off the grid are
+// skipped without a report: a stateless call that returns before its kernel
+// runs has no error word to set (the handle's kernels report off-grid cells
+// as PIC_DEVERR_CELL).
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "pic_internal.cuh"
-
-#define PIC_NOALLOC_MAX_DEVICES 64
 
 // the scratch grid: one int64 accumulator per cell, in 2^-32 charge units
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[PIC_NOALLOC_MAX_CELLS];
 
 namespace {
-
-std::mutex g_setup_mutex;
-unsigned long long *g_scratch_ptr[PIC_NOALLOC_MAX_DEVICES] = {};
 
 __global__ void noalloc_zero_kernel(unsigned long long *acc, long long n)
 {
@@ -73,25 +76,14 @@ __global__ void noalloc_to_double_kernel(const unsigned long long *__restrict__ 
         dst[i] = (double)(long long)acc[i] * scale;
 }
 
-// Device address of the scratch array on the current device, looked up once.
+// Device address of the scratch array on the current device.  In host code
+// g_noalloc_scratch names a host-side stand-in, never the device array.
 pic_status scratch_for_current_device(unsigned long long **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return pic::cuda_fail(e, "pic_deposit_grid_noalloc: cudaGetDevice");
-    if (dev < 0 || dev >= PIC_NOALLOC_MAX_DEVICES) {
-        pic::set_error("pic_deposit_grid_noalloc: device ordinal beyond the supported range");
-        return PIC_ERR_INVALID_ARG;
-    }
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return pic::cuda_fail(e, "pic_deposit_grid_noalloc: cudaGetSymbolAddress");
-        g_scratch_ptr[dev] = (unsigned long long *)p;
-    }
-    *out = g_scratch_ptr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return pic::cuda_fail(e, "pic_deposit_grid_noalloc: cudaGetSymbolAddress");
+    *out = (unsigned long long *)p;
     return PIC_OK;
 }
 

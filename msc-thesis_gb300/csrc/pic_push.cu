@@ -54,295 +54,6 @@ __global__ void __launch_bounds__(256, 4) push_kernel(PushArgs A)
                                            A.anchor[blockIdx.x]);
 }
 
-// ------------------------------------------------------------------------
-// Bulk-copy variant.  Thread 0 streams the chunk into shared memory through
-// a ring of PIPE_STAGES stages of STAGE_PARTICLES particles (five
-// cp.async.bulk copies per stage, completion counted in bytes on the
-// stage's mbarrier); all threads consume the stage from shared memory and
-// store results straight to global memory.  Memory parallelism comes from
-// the stages in flight, not from the number of resident warps.  Every wait
-// is bounded: on expiry the block raises PIC_DEVERR_TIMEOUT, waits (bounded)
-// for the copies it issued and leaves.
-// ------------------------------------------------------------------------
-constexpr int STAGE_PARTICLES = 1024;
-constexpr int PIPE_STAGES = 3;
-constexpr unsigned WAIT_LIMIT = 1u << 20;
-
-__device__ __forceinline__ unsigned smem_u32(const void *p)
-{
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
-{
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity)
-{
-    for (unsigned it = 0; it < WAIT_LIMIT; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
-                                         unsigned long long *bar)
-{
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// shared memory of the bulk-copy variant: the window, the diagnostics, the
-// stage barriers, then the stage ring (16-byte aligned)
-__host__ __device__ __forceinline__ size_t tma_ring_offset(size_t wbytes)
-{
-    return ((wbytes + 32 + PIPE_STAGES * 8) + 127) & ~(size_t)127;
-}
-
-template <bool GATHER, bool DEPOSIT>
-__global__ void __launch_bounds__(256) push_kernel_bulk(PushArgs A)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    const long long n = *A.d_n;
-    const long long base = (long long)blockIdx.x * A.chunk;
-    if (base >= n) return;  // block-uniform
-    const long long n4 = (n + 3) & ~3ll;
-    const long long end = min(base + (long long)A.chunk, n4);
-    const Window W = setup_window(A.geo, smem, A.anchor[blockIdx.x]);
-    const size_t wb = window_bytes(A.geo.wcx, A.geo.wcy);
-    double *sAcc = reinterpret_cast<double *>(smem + wb);
-    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + wb + 32);
-    unsigned char *ring = smem + tma_ring_offset(wb);
-    const int nstages = (int)((end - base + STAGE_PARTICLES - 1) / STAGE_PARTICLES);
-    const size_t field_bytes = (size_t)STAGE_PARTICLES * 4;
-    const size_t stage_bytes = 5 * field_bytes;
-
-    auto issue = [&](int k) {  // thread 0 only
-        const long long s0 = base + (long long)k * STAGE_PARTICLES;
-        const unsigned cnt = (unsigned)min((long long)STAGE_PARTICLES, end - s0);  // multiple of 4
-        const unsigned bytes = cnt * 4u;
-        unsigned char *dst = ring + (size_t)(k % PIPE_STAGES) * stage_bytes;
-        unsigned long long *b = bar + (k % PIPE_STAGES);
-        mbar_expect_tx(b, 5u * bytes);
-        bulk_g2s(dst + 0 * field_bytes, A.cin + s0, bytes, b);
-        bulk_g2s(dst + 1 * field_bytes, A.oxin + s0, bytes, b);
-        bulk_g2s(dst + 2 * field_bytes, A.oyin + s0, bytes, b);
-        bulk_g2s(dst + 3 * field_bytes, A.vxin + s0, bytes, b);
-        bulk_g2s(dst + 4 * field_bytes, A.vyin + s0, bytes, b);
-    };
-
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < PIPE_STAGES; ++k) mbar_init(bar + k, 1u);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    load_window<GATHER, DEPOSIT>(A.geo, W);
-    if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
-    __syncthreads();
-    if (threadIdx.x == 0)
-        for (int k = 0; k < PIPE_STAGES && k < nstages; ++k) issue(k);
-
-    float ke = 0.f, px = 0.f, py = 0.f;
-    bool bad = false;
-    int k = 0;
-    bool timed_out = false;
-    for (; k < nstages; ++k) {
-        const bool ok = mbar_wait_bounded(bar + (k % PIPE_STAGES), (unsigned)((k / PIPE_STAGES) & 1));
-        if (__syncthreads_or(ok ? 0 : 1)) {  // block-uniform decision
-            timed_out = true;
-            break;
-        }
-        const unsigned char *st = ring + (size_t)(k % PIPE_STAGES) * stage_bytes;
-        const long long s0 = base + (long long)k * STAGE_PARTICLES;
-        const int cnt = (int)min((long long)STAGE_PARTICLES, end - s0);
-        for (int l = 4 * threadIdx.x; l < cnt; l += 4 * blockDim.x) {
-            const int4 c4 = *reinterpret_cast<const int4 *>(st + 0 * field_bytes + 4 * l);
-            const float4 a4 = *reinterpret_cast<const float4 *>(st + 1 * field_bytes + 4 * l);
-            const float4 b4 = *reinterpret_cast<const float4 *>(st + 2 * field_bytes + 4 * l);
-            const float4 u4 = *reinterpret_cast<const float4 *>(st + 3 * field_bytes + 4 * l);
-            const float4 v4 = *reinterpret_cast<const float4 *>(st + 4 * field_bytes + 4 * l);
-            int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-            float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
-            float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
-            push_quad<GATHER, DEPOSIT, false>(A.geo, W, cc, xo, yo, xv, yv, ke, px, py, bad);
-            store_quad(A, s0 + l, cc, xo, yo, xv, yv);
-        }
-        __syncthreads();  // every thread is done with this stage's buffer
-        if (threadIdx.x == 0 && k + PIPE_STAGES < nstages) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(k + PIPE_STAGES);
-        }
-    }
-    if (timed_out) {
-        // wait (bounded) for the copies still in flight into this block's
-        // shared memory, report, and leave without flushing partial results
-        if (threadIdx.x == 0) {
-            for (int j = k; j < nstages && j < k + PIPE_STAGES; ++j)
-                mbar_wait_bounded(bar + (j % PIPE_STAGES), (unsigned)((j / PIPE_STAGES) & 1));
-            atomicOr(&A.geo.dev->err, (unsigned)PIC_DEVERR_TIMEOUT);
-        }
-        return;
-    }
-    finish_block<DEPOSIT>(A.geo, W, sAcc, ke, px, py, bad);
-}
-
-// ------------------------------------------------------------------------
-// Warp-specialised pipeline.  One producer warp streams the chunk into a
-// ring of WS_STAGES shared-memory stages of WS_STAGE particles (five
-// cp.async.bulk copies per stage on the bulk-copy engine, completion counted
-// in bytes on the stage's "full" mbarrier); WS_CONSUMERS consumer warps each
-// wait on a stage's full barrier, push one quad per thread straight from
-// shared memory, store the results to global memory and arrive on the
-// stage's "empty" barrier, which the producer waits on before refilling the
-// slot.  No block-wide barrier inside the loop, so the copies of later
-// stages stay in flight while the consumers compute.  Every wait is bounded:
-// on expiry the block raises PIC_DEVERR_TIMEOUT, waits (bounded) for the
-// copies still in flight into its shared memory and leaves without flushing.
-// ------------------------------------------------------------------------
-constexpr int WS_CONSUMERS = 8;
-constexpr int WS_THREADS = 32 * (WS_CONSUMERS + 1);
-constexpr int WS_STAGE = 4 * 32 * WS_CONSUMERS;  // one quad per consumer thread
-// two stages: 3 blocks (24 consumer warps) per SM at 2048^2 x 32 ppc, 1.095
-// ms per push against 1.277 with three or 1.283 with four stages (2 blocks
-// per SM) and 1.046 for the direct kernel's 32 warps, whose latency hiding
-// the consumers' gather and deposit need more than the copies' depth
-constexpr int WS_STAGES = 2;
-
-__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-// the window, the diagnostics, full and empty barriers, then the ring
-__host__ __device__ __forceinline__ size_t ws_ring_offset(size_t wbytes)
-{
-    return ((wbytes + 32 + 2 * WS_STAGES * 8) + 127) & ~(size_t)127;
-}
-
-template <bool GATHER, bool DEPOSIT>
-__global__ void __launch_bounds__(WS_THREADS) push_kernel_ws(PushArgs A)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    const long long n = *A.d_n;
-    const long long base = (long long)blockIdx.x * A.chunk;
-    if (base >= n) return;  // block-uniform
-    const long long n4 = (n + 3) & ~3ll;
-    const long long end = min(base + (long long)A.chunk, n4);
-    const Window W = setup_window(A.geo, smem, A.anchor[blockIdx.x]);
-    const size_t wb = window_bytes(A.geo.wcx, A.geo.wcy);
-    double *sAcc = reinterpret_cast<double *>(smem + wb);
-    unsigned long long *full = reinterpret_cast<unsigned long long *>(smem + wb + 32);
-    unsigned long long *empty = full + WS_STAGES;
-    unsigned char *ring = smem + ws_ring_offset(wb);
-    const int nstages = (int)((end - base + WS_STAGE - 1) / WS_STAGE);
-    constexpr size_t field_bytes = (size_t)WS_STAGE * 4;
-    constexpr size_t stage_bytes = 5 * field_bytes;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < WS_STAGES; ++k) {
-            mbar_init(full + k, 1u);
-            mbar_init(empty + k, (unsigned)WS_CONSUMERS);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    load_window<GATHER, DEPOSIT>(A.geo, W);
-    if (threadIdx.x < 3) sAcc[threadIdx.x] = 0.0;
-    __syncthreads();
-
-    float ke = 0.f, px = 0.f, py = 0.f;
-    bool bad = false, timed_out = false;
-    int issued = 0;
-    if (warp == WS_CONSUMERS) {
-        if (lane == 0) {
-            for (int k = 0; k < nstages; ++k) {
-                const int sl = k % WS_STAGES;
-                if (k >= WS_STAGES) {  // the consumers of stage k - WS_STAGES released the slot
-                    if (!mbar_wait_bounded(empty + sl, (unsigned)((k / WS_STAGES - 1) & 1))) {
-                        timed_out = true;
-                        break;
-                    }
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                }
-                const long long s0 = base + (long long)k * WS_STAGE;
-                const unsigned bytes = (unsigned)min((long long)WS_STAGE, end - s0) * 4u;  // 16-byte multiple
-                unsigned char *dst = ring + (size_t)sl * stage_bytes;
-                mbar_expect_tx(full + sl, 5u * bytes);
-                bulk_g2s(dst + 0 * field_bytes, A.cin + s0, bytes, full + sl);
-                bulk_g2s(dst + 1 * field_bytes, A.oxin + s0, bytes, full + sl);
-                bulk_g2s(dst + 2 * field_bytes, A.oyin + s0, bytes, full + sl);
-                bulk_g2s(dst + 3 * field_bytes, A.vxin + s0, bytes, full + sl);
-                bulk_g2s(dst + 4 * field_bytes, A.vyin + s0, bytes, full + sl);
-                issued = k + 1;
-            }
-        }
-    } else {
-        const int l = 4 * threadIdx.x;  // this thread's quad in every stage
-        for (int k = 0; k < nstages; ++k) {
-            const int sl = k % WS_STAGES;
-            if (!mbar_wait_bounded(full + sl, (unsigned)((k / WS_STAGES) & 1))) {
-                timed_out = true;
-                break;
-            }
-            const long long s0 = base + (long long)k * WS_STAGE;
-            const int cnt = (int)min((long long)WS_STAGE, end - s0);
-            if (l < cnt) {
-                const unsigned char *st = ring + (size_t)sl * stage_bytes;
-                const int4 c4 = *reinterpret_cast<const int4 *>(st + 0 * field_bytes + 4 * l);
-                const float4 a4 = *reinterpret_cast<const float4 *>(st + 1 * field_bytes + 4 * l);
-                const float4 b4 = *reinterpret_cast<const float4 *>(st + 2 * field_bytes + 4 * l);
-                const float4 u4 = *reinterpret_cast<const float4 *>(st + 3 * field_bytes + 4 * l);
-                const float4 v4 = *reinterpret_cast<const float4 *>(st + 4 * field_bytes + 4 * l);
-                int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-                float xo[4] = {a4.x, a4.y, a4.z, a4.w}, yo[4] = {b4.x, b4.y, b4.z, b4.w};
-                float xv[4] = {u4.x, u4.y, u4.z, u4.w}, yv[4] = {v4.x, v4.y, v4.z, v4.w};
-                push_quad<GATHER, DEPOSIT, false>(A.geo, W, cc, xo, yo, xv, yv, ke, px, py, bad);
-                store_quad(A, s0 + l, cc, xo, yo, xv, yv);
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(empty + sl);
-        }
-    }
-    if (__syncthreads_or(timed_out ? 1 : 0)) {
-        // wait (bounded) for the copies still in flight into this block's
-        // shared memory, report, and leave without flushing partial results
-        if (warp == WS_CONSUMERS && lane == 0) {
-            for (int j = max(0, issued - WS_STAGES); j < issued; ++j)
-                mbar_wait_bounded(full + j % WS_STAGES, (unsigned)((j / WS_STAGES) & 1));
-            atomicOr(&A.geo.dev->err, (unsigned)PIC_DEVERR_TIMEOUT);
-        }
-        return;
-    }
-    finish_block<DEPOSIT>(A.geo, W, sAcc, ke, px, py, bad);
-}
-
-size_t push_ws_smem(const Geometry &g)
-{
-    return ws_ring_offset(window_bytes(g.wcx, g.wcy)) + (size_t)WS_STAGES * 5 * WS_STAGE * 4;
-}
-
-// Deposit-only pass (after a sort or an import, before the first step):
-// fixed-point CIC straight to the global density, one particle per thread.
 __global__ void __launch_bounds__(256)
 deposit_flat_kernel(const int32_t *__restrict__ cell, const float *__restrict__ ox,
                     const float *__restrict__ oy, const long long *d_n, long long n_host,
@@ -385,20 +96,6 @@ pic_status allow_dynamic_smem(const void *kernel, size_t bytes)
 {
     if (bytes > 48 * 1024)
         PIC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    return PIC_OK;
-}
-
-size_t push_bulk_smem(const Geometry &g)
-{
-    return tma_ring_offset(window_bytes(g.wcx, g.wcy)) + (size_t)PIPE_STAGES * 5 * STAGE_PARTICLES * 4;
-}
-
-// set on every launch: the attribute belongs to the current device, and a
-// process may drive several
-template <bool G, bool D> static pic_status bulk_attr(size_t sm)
-{
-    PIC_CUDA(cudaFuncSetAttribute(push_kernel_bulk<G, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sm));
     return PIC_OK;
 }
 
@@ -462,42 +159,7 @@ pic_status launch_push(pic_handle *h, int s, int src, bool deposit, float dt_sca
     const bool charged = D.q != 0.0;
     const bool dep = deposit && D.q_int != 0;
     dim3 grid((unsigned)B.nchunks), block(256);
-    if (h->use_bulk) {
-        const size_t sm = push_bulk_smem(g);
-        if (charged && dep) {
-            PIC_TRY((bulk_attr<true, true>(sm)));
-            push_kernel_bulk<true, true><<<grid, block, sm, h->stream>>>(A);
-        } else if (charged) {
-            PIC_TRY((bulk_attr<true, false>(sm)));
-            push_kernel_bulk<true, false><<<grid, block, sm, h->stream>>>(A);
-        } else if (dep) {
-            PIC_TRY((bulk_attr<false, true>(sm)));
-            push_kernel_bulk<false, true><<<grid, block, sm, h->stream>>>(A);
-        } else {
-            PIC_TRY((bulk_attr<false, false>(sm)));
-            push_kernel_bulk<false, false><<<grid, block, sm, h->stream>>>(A);
-        }
-    } else if (h->cfg.push_variant == 4) {
-        const size_t sm = push_ws_smem(g);
-        const dim3 wsb(WS_THREADS);
-        auto attr = [&](const void *f) -> pic_status {
-            PIC_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            return PIC_OK;
-        };
-        if (charged && dep) {
-            PIC_TRY(attr((const void *)push_kernel_ws<true, true>));
-            push_kernel_ws<true, true><<<grid, wsb, sm, h->stream>>>(A);
-        } else if (charged) {
-            PIC_TRY(attr((const void *)push_kernel_ws<true, false>));
-            push_kernel_ws<true, false><<<grid, wsb, sm, h->stream>>>(A);
-        } else if (dep) {
-            PIC_TRY(attr((const void *)push_kernel_ws<false, true>));
-            push_kernel_ws<false, true><<<grid, wsb, sm, h->stream>>>(A);
-        } else {
-            PIC_TRY(attr((const void *)push_kernel_ws<false, false>));
-            push_kernel_ws<false, false><<<grid, wsb, sm, h->stream>>>(A);
-        }
-    } else if (h->cfg.push_variant == 3) {
+    if (h->cfg.push_variant == 3) {
         // warp-summed deposit groups: measured 5% slower at 2048^2 x 32 ppc
         // (1.144 vs 1.085 ms), so opt-in
         const size_t sm = push_smem(g);

@@ -146,6 +146,10 @@ extern "C" pic_status pic_load(pic_handle *h, const char *path)
     const pic_config &c = h->cfg;
     if (nx != c.nx || ny != c.ny || Lx != c.Lx || Ly != c.Ly || ns != c.nspecies)
         return io_fail("pic_load: grid or species count differs from the handle's");
+    // a resumed run continues bit for bit only under the same step and
+    // permittivity, so a file written under others is refused
+    if (dt != c.dt || eps0 != c.eps0)
+        return io_fail("pic_load: time step or permittivity differs from the handle's");
     long long n[PIC_MAX_SPECIES] = {0, 0, 0, 0};
     for (int s = 0; s < ns; ++s) {
         int flags, q_int;
@@ -153,9 +157,10 @@ extern "C" pic_status pic_load(pic_handle *h, const char *path)
         if (!get(f, n[s]) || !get(f, flags) || !get(f, q_int) || !get(f, q) || !get(f, m))
             return io_fail("pic_load: file truncated");
         const pic_species_desc &D = c.species[s];
-        if (n[s] < 0 || n[s] > D.capacity || flags != D.flags || q_int != D.q_int)
+        if (n[s] < 0 || n[s] > D.capacity || flags != D.flags || q_int != D.q_int || q != D.q ||
+            m != D.m)
             return io_fail("pic_load: species " + std::to_string(s) +
-                           " does not fit the handle (count, flags or charge)");
+                           " does not fit the handle (count, flags, charge or mass)");
     }
     // read and check everything before the handle is touched, so that a bad
     // file leaves it as it was

@@ -251,6 +251,25 @@ def mcc_pass(m: dict, pid, vx, vy, vz, pass_no, cap_new=None):
     return vx, vy, vz, ne[:born], ni[:born], parent[:born], counts
 
 
+def mcc_passes(m: dict, pid, vx, vy, vz, first_pass, npasses, nthreads=0):
+    """npasses MCC passes over fixed electrons (no field, newborns not kept):
+    returns (vx, vy, vz, counts)."""
+    L = lib()
+    L.orc_mcc_passes.restype = None
+    L.orc_mcc_passes.argtypes = [C.POINTER(MccC), C.c_long, C.c_void_p, _dp, _dp, _dp,
+                                 C.c_uint64, C.c_long, C.c_void_p, C.c_int]
+    tabs = [np.ascontiguousarray(m[k], dtype=np.float64) for k in ("sel", "sexc", "sion")]
+    mc = MccC(len(tabs[0]), m["e_min"], m["e_max"], *[_p(t) for t in tabs], m["ng"],
+              m["half_me_over_e"], m["two_m_over_M"], m["e_exc"], m["e_ion"], m["vth_ion"],
+              m["nu_max"], m["p_null"], m["seed"])
+    vx, vy, vz = (np.array(a, dtype=np.float64) for a in (vx, vy, vz))
+    pid = np.ascontiguousarray(pid, dtype=np.uint32)
+    counts = np.zeros(4, dtype=np.int64)
+    L.orc_mcc_passes(C.byref(mc), len(vx), pid.ctypes.data, _p(vx), _p(vy), _p(vz), first_pass,
+                     npasses, counts.ctypes.data, nthreads)
+    return vx, vy, vz, counts
+
+
 def dsmc_run(d: dict, x, y, vx, vy, vz, sgmax, nsteps, first_pass=0):
     L = lib()
     L.orc_dsmc_run.restype = None

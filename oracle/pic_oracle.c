@@ -698,64 +698,111 @@ static void mcc_sigmas(const orc_mcc *m, double E, double *sel, double *sexc, do
     *sion = m->sion[k] + f * (m->sion[k + 1] - m->sion[k]);
 }
 
+/* One electron's null-collision test and collision in pass `pass`
+ * (velocity in/out).  Returns the process (0 elastic, 1 excitation,
+ * 2 ionisation, 3 null, -1 not a candidate); for an ionisation with ej
+ * and ion non-NULL, the ejected electron's and the ion's velocities. */
+static int mcc_one(const orc_mcc *m, uint32_t pid, uint64_t pass, double *pvx, double *pvy,
+                   double *pvz, double ej[3], double ion[3])
+{
+    uint32_t r[4];
+    philox_u4(pid, (uint32_t)pass, 0u, STREAM_MCC, m->seed, r);
+    if (u24(r[0]) >= m->p_null) return -1;
+    double vx = *pvx, vy = *pvy, vz = *pvz;
+    double v2 = vx * vx + vy * vy + vz * vz;
+    double v = sqrt(v2), E = m->half_me_over_e * v2;
+    double sel, sexc, sion;
+    mcc_sigmas(m, E, &sel, &sexc, &sion);
+    if (E < m->e_exc) sexc = 0.0;
+    if (E < m->e_ion) sion = 0.0;
+    double nel = m->ng * sel * v, nexc = m->ng * sexc * v, nion = m->ng * sion * v;
+    double R = u24(r[1]) * m->nu_max;
+    double ux = v > 0 ? vx / v : 0.0, uy = v > 0 ? vy / v : 0.0, uz = v > 0 ? vz / v : 1.0;
+    double d[3], vn;
+    int proc;
+    if (R < nel) {
+        double c = 1.0 - 2.0 * u24(r[2]);
+        double En = E * (1.0 - m->two_m_over_M * (1.0 - c));
+        deflect(ux, uy, uz, c, u24(r[3]), d);
+        vn = sqrt(En / m->half_me_over_e);
+        proc = 0;
+    } else if (R < nel + nexc) {
+        deflect(ux, uy, uz, 1.0 - 2.0 * u24(r[2]), u24(r[3]), d);
+        vn = sqrt(fmax(E - m->e_exc, 0.0) / m->half_me_over_e);
+        proc = 1;
+    } else if (R < nel + nexc + nion) {
+        uint32_t r2[4], r3[4];
+        philox_u4(pid, (uint32_t)pass, 1u, STREAM_MCC, m->seed, r2);
+        double Er = fmax(E - m->e_ion, 0.0), Ej = u24(r2[0]) * Er, Es = Er - Ej;
+        double dj[3];
+        deflect(ux, uy, uz, 1.0 - 2.0 * u24(r[2]), u24(r[3]), d);
+        deflect(ux, uy, uz, 1.0 - 2.0 * u24(r2[1]), u24(r2[2]), dj);
+        vn = sqrt(Es / m->half_me_over_e);
+        double vj = sqrt(Ej / m->half_me_over_e);
+        if (ej && ion) {
+            philox_u4(pid, (uint32_t)pass, 2u, STREAM_MCC, m->seed, r3);
+            double ra = sqrt(-2.0 * log(u24(r3[0]))), rb = sqrt(-2.0 * log(u24(r3[2])));
+            for (int k = 0; k < 3; ++k) ej[k] = vj * dj[k];
+            ion[0] = m->vth_ion * ra * cos(2.0 * M_PI * u24(r3[1]));
+            ion[1] = m->vth_ion * ra * sin(2.0 * M_PI * u24(r3[1]));
+            ion[2] = m->vth_ion * rb * cos(2.0 * M_PI * u24(r3[3]));
+        }
+        proc = 2;
+    } else {
+        return 3;
+    }
+    *pvx = vn * d[0];
+    *pvy = vn * d[1];
+    *pvz = vn * d[2];
+    return proc;
+}
+
 long orc_mcc_pass(const orc_mcc *m, long n, const uint32_t *pid, double *vx, double *vy,
                   double *vz, uint64_t pass, long cap_new, double *new_e, double *new_i,
                   long *parent, long counts[4])
 {
     long born = 0;
     for (long i = 0; i < n; ++i) {
-        uint32_t r[4];
-        philox_u4(pid[i], (uint32_t)pass, 0u, STREAM_MCC, m->seed, r);
-        if (u24(r[0]) >= m->p_null) continue;
-        double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
-        double v = sqrt(v2), E = m->half_me_over_e * v2;
-        double sel, sexc, sion;
-        mcc_sigmas(m, E, &sel, &sexc, &sion);
-        if (E < m->e_exc) sexc = 0.0;
-        if (E < m->e_ion) sion = 0.0;
-        double nel = m->ng * sel * v, nexc = m->ng * sexc * v, nion = m->ng * sion * v;
-        double R = u24(r[1]) * m->nu_max;
-        double ux = v > 0 ? vx[i] / v : 0.0, uy = v > 0 ? vy[i] / v : 0.0, uz = v > 0 ? vz[i] / v : 1.0;
-        double d[3], vn;
-        if (R < nel) {
-            double c = 1.0 - 2.0 * u24(r[2]);
-            double En = E * (1.0 - m->two_m_over_M * (1.0 - c));
-            deflect(ux, uy, uz, c, u24(r[3]), d);
-            vn = sqrt(En / m->half_me_over_e);
-            counts[0]++;
-        } else if (R < nel + nexc) {
-            deflect(ux, uy, uz, 1.0 - 2.0 * u24(r[2]), u24(r[3]), d);
-            vn = sqrt(fmax(E - m->e_exc, 0.0) / m->half_me_over_e);
-            counts[1]++;
-        } else if (R < nel + nexc + nion) {
-            uint32_t r2[4], r3[4];
-            philox_u4(pid[i], (uint32_t)pass, 1u, STREAM_MCC, m->seed, r2);
-            double Er = fmax(E - m->e_ion, 0.0), Ej = u24(r2[0]) * Er, Es = Er - Ej;
-            double dj[3];
-            deflect(ux, uy, uz, 1.0 - 2.0 * u24(r[2]), u24(r[3]), d);
-            deflect(ux, uy, uz, 1.0 - 2.0 * u24(r2[1]), u24(r2[2]), dj);
-            vn = sqrt(Es / m->half_me_over_e);
-            double vj = sqrt(Ej / m->half_me_over_e);
-            counts[2]++;
-            if (born < cap_new) {
-                philox_u4(pid[i], (uint32_t)pass, 2u, STREAM_MCC, m->seed, r3);
-                double ra = sqrt(-2.0 * log(u24(r3[0]))), rb = sqrt(-2.0 * log(u24(r3[2])));
-                for (int k = 0; k < 3; ++k) new_e[3 * born + k] = vj * dj[k];
-                new_i[3 * born + 0] = m->vth_ion * ra * cos(2.0 * M_PI * u24(r3[1]));
-                new_i[3 * born + 1] = m->vth_ion * ra * sin(2.0 * M_PI * u24(r3[1]));
-                new_i[3 * born + 2] = m->vth_ion * rb * cos(2.0 * M_PI * u24(r3[3]));
-                parent[born] = i;
-                born++;
+        double ej[3], ion[3];
+        int keep = born < cap_new;
+        int proc = mcc_one(m, pid[i], pass, &vx[i], &vy[i], &vz[i], keep ? ej : NULL,
+                           keep ? ion : NULL);
+        if (proc < 0) continue;
+        counts[proc]++;
+        if (proc == 2 && keep) {
+            for (int k = 0; k < 3; ++k) {
+                new_e[3 * born + k] = ej[k];
+                new_i[3 * born + k] = ion[k];
             }
-        } else {
-            counts[3]++;
-            continue;
+            parent[born] = i;
+            born++;
         }
-        vx[i] = vn * d[0];
-        vy[i] = vn * d[1];
-        vz[i] = vn * d[2];
     }
     return born;
+}
+
+void orc_mcc_passes(const orc_mcc *m, long n, const uint32_t *pid, double *vx, double *vy,
+                    double *vz, uint64_t first_pass, long npasses, long counts[4], int nthreads)
+{
+    long c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    nthreads = clamp_threads(nthreads);
+#pragma omp parallel for num_threads(nthreads) schedule(static) reduction(+ : c0, c1, c2, c3)
+    for (long i = 0; i < n; ++i) {
+        for (long p = 0; p < npasses; ++p) {
+            switch (mcc_one(m, pid[i], first_pass + (uint64_t)p, &vx[i], &vy[i], &vz[i], NULL,
+                            NULL)) {
+            case 0: c0++; break;
+            case 1: c1++; break;
+            case 2: c2++; break;
+            case 3: c3++; break;
+            default: break;
+            }
+        }
+    }
+    counts[0] += c0;
+    counts[1] += c1;
+    counts[2] += c2;
+    counts[3] += c3;
 }
 
 static void group_temps(long n, const double *vx, const double *vy, const double *vz, double mass,

@@ -114,6 +114,13 @@ long orc_mcc_pass(const orc_mcc *m, long n, const uint32_t *pid, double *vx, dou
                   double *vz, uint64_t pass, long cap_new, double *new_e, double *new_i,
                   long *parent, long counts[4]);
 
+/* npasses MCC passes (first_pass, first_pass + 1, ...) over n electrons
+ * whose ids and velocities persist between passes (velocities in/out), with
+ * no field between passes; ionisations scatter the parent but their new
+ * particles are not kept.  counts accumulate as for orc_mcc_pass. */
+void orc_mcc_passes(const orc_mcc *m, long n, const uint32_t *pid, double *vx, double *vy,
+                    double *vz, uint64_t first_pass, long npasses, long counts[4], int nthreads);
+
 /* DSMC (hard spheres, Bird's NTC) of one neutral species with free
  * streaming, nsteps steps: each step groups particles by cell (cx + cy*nx),
  * collides per cell, then moves x += v dt (periodic).  sgmax: per cell,

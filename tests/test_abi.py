@@ -60,6 +60,13 @@ def test_config_validation_is_host_side():
     with pytest.raises(P.PicError) as e:
         P.Handle(bad)
     assert e.value.status == 1
+    # the bulk-copy push pipelines (variants 2 and 4) were removed
+    for variant in (2, 4, -1):
+        bad = P.config(64, 64, 1.0, 1.0, 0.1, [P.species(100, -1.0, 1.0, -1)],
+                       push_variant=variant)
+        with pytest.raises(P.PicError) as e:
+            P.Handle(bad)
+        assert e.value.status == 1
 
 
 def test_compat_params_validation_is_host_side():

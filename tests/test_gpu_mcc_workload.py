@@ -1,0 +1,81 @@
+"""The MCC workload at its stated size and horizon: 512 x 512 cells, 64
+electrons and 64 ions (mass ratio 1/73,000) per cell, Te0 = 2 eV, the
+tabulated elastic, excitation and ionisation cross sections against
+3.2e21 m^-3 neutrals at 300 K, null-collision MCC after every push, 5000
+steps of dt = 1e-11 s.  The MCC pass fills the slot of the reference's
+collision call in its step loop (mccCollisions/src/main.cc:180-183).
+
+The oracle is the C restatement of the MCC pass (orc_mcc_passes), run on
+the first K electrons from their initial velocities through the same 5000
+passes on the same Philox streams (keyed by particle id and pass).  The
+restatement has no field between passes, so the comparison is statistical:
+the energy distributions of those K electrons, and the process counts of
+all electrons against the oracle's per-electron rates."""
+import numpy as np
+import pytest
+
+import oracle as O
+import picgpu as P
+from collide_util import (E_CH, ME, MI, NG, TN_EV, energies_eV, ks_statistic, mcc_resolved,
+                          set_tabulated_mcc)
+
+pytestmark = pytest.mark.gpu
+
+NX = 512
+DX = 2e-4
+DT = 1e-11
+NSTEPS = 5000
+K = 200_000
+
+
+def test_mcc_workload_5000_steps_against_the_restatement():
+    L = NX * DX
+    ne = NX * NX * 64
+    w = 1e15 * L * L / ne
+    sp = [P.species(ne + ne // 4, -E_CH * w, ME * w, -1, P.SPECIES_HAS_VZ),
+          P.species(ne + ne // 4, E_CH * w, MI * w, 1, P.SPECIES_HAS_VZ)]
+    cfg = P.config(NX, NX, L, L, DT, sp, eps0=8.8541878128e-12, sort_every=40)
+    ve, vi = np.sqrt(2.0 * E_CH / ME), np.sqrt(TN_EV * E_CH / MI)
+    seed = 9
+    with P.Handle(cfg) as h:
+        h.init_particles(0, P.init_spec(ne, vth=(ve, ve, ve), seed=5))
+        h.init_particles(1, P.init_spec(ne, vth=(vi, vi, vi), seed=6))
+        set_tabulated_mcc(h, seed)
+        a0 = h.get_particles(0, vz=True)
+        h.prime_leapfrog()
+        h.step(NSTEPS)
+        h.synchronize()
+        d = h.diagnostics()
+        c = np.array(h.collision_counts()[:4], dtype=np.int64)
+        q = h.history(P.HIST_CHARGE, 0, NSTEPS + 1)
+        a1 = h.get_particles(0, vz=True)
+    assert d.error_flags == 0
+    assert (q == 0.0).all() and d.total_charge_fixed == d.expected_charge_fixed
+    born = int(d.n[0]) - ne
+    assert born == int(d.n[1]) - ne == c[2]
+    m = mcc_resolved(DT, seed)
+    pid = np.arange(K)
+    vx, vy, vz, oc = O.mcc_passes(m, pid, a0["vx"][:K], a0["vy"][:K], a0["vz"][:K], 1, NSTEPS)
+    eo = energies_eV(dict(vx=vx, vy=vy, vz=vz))
+    eg = energies_eV({k: a1[k][:K] for k in ("vx", "vy", "vz")})
+    e_init = energies_eV({k: a0[k][:K] for k in ("vx", "vy", "vz")})
+    D = ks_statistic(eg, eo)
+    D0 = ks_statistic(e_init, eo)
+    scale = ne / K
+    print(f"{NSTEPS} steps: GPU counts {c.tolist()} (born {born}); oracle on {K} electrons "
+          f"{oc.tolist()} x {scale:.1f} = {(oc * scale).round().tolist()}")
+    print(f"mean energy: initial {e_init.mean():.5f}, gpu {eg.mean():.5f}, oracle {eo.mean():.5f} eV; "
+          f"KS gpu vs oracle {D:.5f}, initial vs oracle {D0:.5f}, critical (0.1 %) "
+          f"{1.95 * np.sqrt(2.0 / K):.5f}")
+    tail_g, tail_o = np.mean(eg > 11.5), np.mean(eo > 11.5)
+    print(f"fraction above the excitation threshold: initial {np.mean(e_init > 11.5):.3e}, "
+          f"gpu {tail_g:.3e}, oracle {tail_o:.3e}")
+    assert D < 1.95 * np.sqrt(2.0 / K)
+    assert abs(eg.mean() - eo.mean()) < 2e-3 * eo.mean()
+    # elastic collisions are frequent (about 7 per electron): their rate, scaled
+    # from the K electrons to all, within 3 sigma of the sampling error
+    # plus 0.5 % for the field's change of the electrons' speeds
+    for k in (0, 1):
+        exp_k = oc[k] * scale
+        sig = np.sqrt(oc[k]) * scale
+        assert abs(c[k] - exp_k) < 3 * sig + 5e-3 * exp_k, k

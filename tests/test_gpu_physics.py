@@ -37,8 +37,8 @@ def test_short_run_matches_fp64_oracle():
         dxp = periodic_diff(a["x"], s["x"], L)
         dyp = periodic_diff(a["y"], s["y"], L)
         print("position max abs err (cells)", np.abs(dxp).max() / (L / nx))
-        assert np.abs(dxp).max() < 1e-3 * L / nx
-        assert np.abs(dyp).max() < 1e-3 * L / ny
+        assert np.abs(dxp).max() < 3e-5 * L / nx  # measured 2.4e-6 cells
+        assert np.abs(dyp).max() < 3e-5 * L / ny
         np.testing.assert_allclose(a["vx"], s["vx"], atol=1e-4 * np.abs(s["vx"]).max())
 
 
@@ -159,28 +159,8 @@ def test_odd_grids_match_fp64_oracle(nx, ny):
         a = h.get_particles()
     rel = np.abs(fe - ref["fe"]) / ref["fe"].max()
     print(nx, ny, "field energy max rel err", rel.max())
-    assert rel.max() < 2e-4
+    assert rel.max() < 1e-5  # measured 4e-7 and 8e-7
     assert d.total_charge_fixed == d.expected_charge_fixed
     s = st.species[0]
-    assert np.abs(periodic_diff(a["x"], s["x"], Lx)).max() < 1e-3 * Lx / nx
-    assert np.abs(periodic_diff(a["y"], s["y"], Ly)).max() < 1e-3 * Ly / ny
-
-
-def test_pipelined_push_variants_match_direct_loads():
-    """Bulk-copy pipelines (push_variant 2: block-wide stages; 4: producer
-    warp and consumer warps on mbarriers) give the direct kernel's state bit
-    for bit: 8 stages per block (the 4-slot ring wraps), a partial last
-    stage, sorts every 5 steps."""
-    nx, ny = 64, 32
-    n = nx * ny * 20 + 148
-    states = {}
-    for variant in (1, 2, 4):
-        cfg, _, _ = normalized_electrons(nx, ny, 8.0, 4.0, n, 0.1, sort_every=5, chunk=8192,
-                                         push_variant=variant)
-        states[variant] = run_state(cfg, n, 12, seed=7)
-    for variant in (2, 4):
-        for k in states[1][0]:
-            np.testing.assert_array_equal(states[1][0][k], states[variant][0][k],
-                                          err_msg=f"variant {variant} {k}")
-        np.testing.assert_array_equal(states[1][1], states[variant][1])
-        np.testing.assert_array_equal(states[1][2], states[variant][2])
+    assert np.abs(periodic_diff(a["x"], s["x"], Lx)).max() < 3e-5 * Lx / nx
+    assert np.abs(periodic_diff(a["y"], s["y"], Ly)).max() < 3e-5 * Ly / ny

@@ -78,6 +78,10 @@ def test_bad_files_are_rejected_and_leave_the_handle_unchanged(tmp_path):
         "truncated": lambda r: r[:-3],
         "trailing": lambda r: r + b"\0",
         "grid": lambda r: r[:12] + struct.pack("<i", NX * 2) + r[16:],
+        "dt": lambda r: r[:36] + struct.pack("<d", 0.05) + r[44:],
+        "eps0": lambda r: r[:44] + struct.pack("<d", 2.0) + r[52:],
+        "charge": lambda r: r[:HEADER + 16] + struct.pack("<d", -1.0) + r[HEADER + 24:],
+        "mass": lambda r: r[:HEADER + 24] + struct.pack("<d", 1.0) + r[HEADER + 32:],
         "count": lambda r: r[:HEADER] + struct.pack("<q", n + 1) + r[HEADER + 8:],
         "cell": lambda r: r[:body] + struct.pack("<i", NX) + r[body + 4:],
         "offset": lambda r: r[:body + 4 * n] + struct.pack("<f", 1.0) + r[body + 4 * n + 4:],

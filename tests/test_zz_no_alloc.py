@@ -19,6 +19,7 @@ def _particles(rng, nx, ny, n):
     cx, cy = rng.integers(0, nx, n), rng.integers(0, ny, n)
     cell = (cx | (cy << 16)).astype(np.int32)
     cell[::101] = -1  # empty slots are skipped
+    cell[5::997] = nx | (cy[5::997] << 16)  # off the grid: skipped by both calls
     return cell, rng.random(n, dtype=np.float32), rng.random(n, dtype=np.float32)
 
 
