@@ -34,7 +34,8 @@ def test_mcc_workload_5000_steps_against_the_restatement():
     w = 1e15 * L * L / ne
     sp = [P.species(ne + ne // 4, -E_CH * w, ME * w, -1, P.SPECIES_HAS_VZ),
           P.species(ne + ne // 4, E_CH * w, MI * w, 1, P.SPECIES_HAS_VZ)]
-    cfg = P.config(NX, NX, L, L, DT, sp, eps0=8.8541878128e-12, sort_every=40)
+    cfg = P.config(NX, NX, L, L, DT, sp, eps0=8.8541878128e-12, sort_every=40,
+                   history=NSTEPS + 1)
     ve, vi = np.sqrt(2.0 * E_CH / ME), np.sqrt(TN_EV * E_CH / MI)
     seed = 9
     with P.Handle(cfg) as h:
