@@ -84,13 +84,26 @@ def test_ensemble_independent_of_sort_cadence():
             np.testing.assert_array_equal(out[0][r][k], out[1][r][k], err_msg=f"run {r} {k}")
 
 
-def test_ensemble_field_energy_matches_fp64_oracle():
-    """Each run's field-energy history over 200 steps (through the growth and
-    the saturation of the instability) against the FP64 oracle from the same
-    load, relative to the run's largest field energy: within 1e-5."""
-    runs = [(32, 32, 16, 0.2, 1e-2, 7), (16, 32, 32, 0.25, 1e-2, 8), (128, 128, 16, 0.15, 1e-3, 9)]
-    nst = 200
-    cfgs, specs = build(runs)
+@pytest.mark.parametrize("runs,nst,bar", [
+    ([(32, 32, 16, 0.2, 1e-2, 7), (16, 32, 32, 0.25, 1e-2, 8), (128, 128, 16, 0.15, 1e-3, 9)],
+     200, 1e-5),
+    ([(64, 64, 32, 0.286, 5.4e-4, 10), (128, 128, 64, 0.145, 1.1e-3, 11)], 500, 1e-5),
+    ([(64, 64, 16, 0.13, 5.8e-4, 12)], 500, 3e-5)])
+def test_ensemble_field_energy_matches_fp64_oracle(runs, nst, bar):
+    """Each run's field-energy history against the FP64 oracle from the same
+    load, relative to the run's largest field energy.  Within 1e-5 over 200
+    steps (through the growth and the saturation of the instability) for all
+    sizes, and over the batched configuration's 500 steps for its runs of 32
+    and more particles per cell.  After saturation the orbits are chaotic and
+    the FP32 run (2^-16-cell deposit weights, FP32 offsets and velocities)
+    drifts from the FP64 one by about 4x per 100 steps: the configuration's
+    smallest runs (64^2 x 16 per cell, 65,536 particles) end at 1.4e-5 to
+    2.1e-5 after 500 steps."""
+    cfgs, specs = [], []
+    for nx, ny, ppc, v0, amp, seed in runs:
+        cfg, n, _, _ = run_cfg(nx, ny, ppc, history=nst + 1)
+        cfgs.append(cfg)
+        specs.append(run_spec(n, v0, amp, seed))
     with P.Ensemble(cfgs) as E:
         E.init(specs)
         E.step(nst)
@@ -103,9 +116,11 @@ def test_ensemble_field_energy_matches_fp64_oracle():
         st.prime(nthreads=0)
         ref = st.run(nst, nthreads=0)
         rel = np.abs(fe_ens[r] - ref["fe"]) / ref["fe"].max()
-        print(f"run {r}: field energy max rel error vs FP64 oracle "
-              + ", ".join(f"{k} steps {rel[:k + 1].max():.2e}" for k in (40, 100, 200)))
-        assert rel.max() < 1e-5  # measured up to 1.5e-6
+        print(f"{nx}x{ny} x {ppc}: field energy max rel error vs FP64 oracle "
+              + ", ".join(f"{k} steps {rel[:k + 1].max():.2e}" for k in (40, 100, 200, 300, 400, 500)
+                          if k <= nst))
+        assert rel[:201].max() < 1e-5
+        assert rel.max() < bar
 
 
 def test_ensemble_rejects_bad_configs():
