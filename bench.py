@@ -206,6 +206,7 @@ def fp64_check(P, cfg, spec, q, m, nsteps):
     same loaded particles, over the first nsteps steps (untimed)."""
     import numpy as np
 
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     with P.Handle(cfg) as h:
