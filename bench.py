@@ -424,6 +424,11 @@ def ensemble_record(P, R, torch, local, steps=80, adjoint_steps=100, every=50, f
                                PLAIN_TUNED, None, local)
     ens_v = total * m["steps"] / (m["ms"] / 1000.0)
     plain_v = total * m["steps"] / (m["plain_ms"] / 1000.0)
+    # the most any batching could gain: the runs' algorithmic bytes per step
+    # moved at the measured copy bandwidth, against the plain runs' time
+    hbm, peak_kind = peaks()
+    cells = sum(int(g) * int(g) for g in grids)
+    floor_ms = (BYTES_PER_PARTICLE * total + BYTES_PER_CELL * cells) / (hbm * 1e9) * 1e3
     adj = ensemble_adjoint_rate(P, R, cfgs, specs, total, adjoint_steps, every, None) \
         if adjoint_steps else None
     return {"workload": "ensemble-64-two-stream", "runs": len(cfgs), "particles": total,
@@ -432,6 +437,9 @@ def ensemble_record(P, R, torch, local, steps=80, adjoint_steps=100, every=50, f
             "chunk": ENSEMBLE_TUNED[0], "sort_every": m["S"],
             "plain_sequential": {"value": plain_v, "ms_per_step": m["plain_ms"] / m["steps"]},
             "speedup_vs_plain": ens_v / plain_v, "charge_exact": m["charge_ok"],
+            "roofline_ms_per_step": floor_ms,
+            "speedup_bound": m["plain_ms"] / m["steps"] / floor_ms,
+            "roofline_frac": floor_ms / (m["ms"] / m["steps"]), "peak_kind": peak_kind,
             "batched_adjoint": adj,
             "fp64_check": ens_fp64_check(P, cfgs, specs, 10) if fp64 else None,
             "clocks": m["clocks"],

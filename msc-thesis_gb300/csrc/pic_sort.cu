@@ -18,7 +18,15 @@
 // by a whole tile row in key space; those stragglers are counted in a small
 // open-addressing hash table in shared memory (again one global atomic per
 // distinct key and block), and only when its bounded probe fails does a
-// particle fall back to a global atomic of its own.
+// run of particles fall back to global atomics of its own.
+// Each thread owns eight consecutive particles (128-bit loads of every
+// field); the runs of equal keys among them are counted with one shared
+// atomic each, whose result is also the run's rank among the block's
+// particles of that key, so the scatter counts and ranks in one pass.  The
+// scatter then stages every particle as one 32-byte record in shared memory
+// in destination order (two 128-bit stores and loads per particle, the
+// record rows XOR-swizzled against bank conflicts) and writes the fields
+// out with consecutive threads on consecutive slots.
 // After the scatter, offset[key] .. offset[key+1] is the slice of cell `key`
 // and every push chunk knows the tile of its first particle (anchor).
 #include <cuda_runtime.h>
@@ -39,7 +47,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
     sort_hist_block(A, single_geo(A), S, base, n);
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 4) sort_scatter_kernel(SortArgs A)
+__global__ void __launch_bounds__(SORT_THREADS, 3) sort_scatter_kernel(SortArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem);

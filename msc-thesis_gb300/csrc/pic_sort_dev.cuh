@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cstddef>
 
 #include "pic_internal.cuh"
@@ -80,6 +81,10 @@ __device__ __forceinline__ KeyGeo single_geo(const SortArgs &A)
     return key_geo(A.nx, A.ny, A.tw, A.th, A.ntx, 0);
 }
 
+// Work of a sort block: SORT_CHUNK consecutive particles, thread t owning the
+// SORT_PER_THREAD consecutive particles base + 8t ... base + 8t + 7, read
+// with 128-bit loads (base is a multiple of 4 particles, so each half of a
+// thread's eight is 16-byte aligned).
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_PER_THREAD = 8;
 constexpr int SORT_CHUNK = SORT_THREADS * SORT_PER_THREAD;
@@ -157,13 +162,13 @@ __device__ __forceinline__ int window_start(const SortArgs &A, const KeyGeo &G, 
     return max(0, k - wk / 2);
 }
 
-// Shared state of one sort block: dense window counts and the straggler table.
+// Counting state of one sort block: dense window counts and the straggler
+// table.  The scatter keeps, per window key and table slot, the first slot
+// of its global slice (gb) and of its block-local staging range (lb).
 struct SortSmem {
     uint32_t cnt[SORT_KEYS];
-    uint32_t base[SORT_KEYS];
     int hkey[HASH_SLOTS];
     uint32_t hcnt[HASH_SLOTS];
-    uint32_t hbase[HASH_SLOTS];
 };
 
 __device__ __forceinline__ void init_smem(SortSmem &S, SortSizes Z)
@@ -175,99 +180,100 @@ __device__ __forceinline__ void init_smem(SortSmem &S, SortSizes Z)
     }
 }
 
-// Runs of equal keys across the 32 lanes of a warp (lanes hold consecutive
-// particles, so in nearly sorted data a warp holds one or two runs).  Built
-// from full-warp shuffles and ballots only: the head lane of each run does
-// one atomic for the whole run and every lane knows its rank in the run.
-struct Run {
-    bool head;
-    int hidx;  // lane of the run's head
-    int len;   // run length (meaningful on the head)
-    int rank;  // position of this lane in its run
-};
-
-// a Run in one word (head bit 0, head lane bits 1-5, length bits 6-11,
-// rank bits 12-16), kept from the count to the ranking phase
-__device__ __forceinline__ int pack_run(const Run &r)
-{
-    return (int)r.head | (r.hidx << 1) | (r.len << 6) | (r.rank << 12);
-}
-
-__device__ __forceinline__ Run unpack_run(int w)
-{
-    Run r;
-    r.head = w & 1;
-    r.hidx = (w >> 1) & 31;
-    r.len = (w >> 6) & 63;
-    r.rank = (w >> 12) & 31;
-    return r;
-}
-
-__device__ __forceinline__ Run warp_run(int key)
-{
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int prev = __shfl_up_sync(full, key, 1);
-    const bool head = (lane == 0) || (key != prev);
-    const unsigned heads = __ballot_sync(full, head);
-    const unsigned upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
-    const unsigned above = heads & ~upto;
-    Run r;
-    r.head = head;
-    r.hidx = 31 - __clz(heads & upto);
-    r.len = (above ? __ffs(above) - 1 : 32) - lane;
-    r.rank = lane - r.hidx;
-    return r;
-}
-
-// Cells of this thread's particles (-1 past the end), loaded before the
-// window setup so that the two loads' latencies overlap.
+// The thread's eight cells (two 128-bit loads); slots at or past `end` get
+// INT_MIN (no particle).
 __device__ __forceinline__ void load_cells(const SortArgs &A, long long base, long long end,
                                            int (&cells)[SORT_PER_THREAD])
 {
+    const long long p0 = base + (long long)SORT_PER_THREAD * threadIdx.x;
 #pragma unroll
-    for (int j = 0; j < SORT_PER_THREAD; ++j) {
-        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
-        cells[j] = (i < end) ? A.cin[i] : -1;
+    for (int h = 0; h < 2; ++h) {
+        const long long q = p0 + 4 * h;
+        int4 c = make_int4(INT_MIN, INT_MIN, INT_MIN, INT_MIN);
+        if (q < end) c = *reinterpret_cast<const int4 *>(A.cin + q);
+        cells[4 * h + 0] = c.x;
+        cells[4 * h + 1] = q + 1 < end ? c.y : INT_MIN;
+        cells[4 * h + 2] = q + 2 < end ? c.z : INT_MIN;
+        cells[4 * h + 3] = q + 3 < end ? c.w : INT_MIN;
     }
 }
 
-// Pass 1 of both kernels: keys of this thread's particles (`keys` holds
-// their cells from load_cells on entry), counted in the window or the
-// table; a run the table had no room for gets FALLBACK_BIT (on all its
-// lanes, so the runs stay the same).  KEEP: each key's run, packed, to
-// `runs` for the ranking phase.
-template <bool KEEP>
-__device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, SortSmem &S,
-                                           long long base, long long end, int k0, SortSizes Z,
-                                           int (&keys)[SORT_PER_THREAD], int (&runs)[SORT_PER_THREAD])
+// Length of the run of equal keys that starts at particle j of the thread's
+// eight consecutive particles (compile-time indices only).
+template <int J>
+__device__ __forceinline__ int run_length(const int (&keys)[SORT_PER_THREAD])
 {
+    int l = 1;
+    bool same = true;
 #pragma unroll
-    for (int j = 0; j < SORT_PER_THREAD; ++j) {
-        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
-        keys[j] = (i < end) ? particle_key(G, A.err, keys[j]) : -1;
+    for (int k = J + 1; k < SORT_PER_THREAD; ++k) {
+        same = same && keys[k] == keys[J];
+        l += same ? 1 : 0;
     }
-#pragma unroll
-    for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
-        const int key = keys[j];
-        const Run R = warp_run(key);
-        int fb = 0;
-        if (R.head && key >= 0) {
-            const unsigned r = (unsigned)(key - k0);
-            if (r < (unsigned)Z.wk) {
-                atomicAdd(S.cnt + r, (uint32_t)R.len);
+    return l;
+}
+
+template <int J>
+__device__ __forceinline__ bool run_head(const int (&keys)[SORT_PER_THREAD])
+{
+    return keys[J] >= 0 && (J == 0 || keys[J] != keys[J > 0 ? J - 1 : 0]);
+}
+
+// Pass 1 of both kernels: the keys of the thread's particles (`keys` holds
+// their cells on entry; INT_MIN becomes -1), each run of equal keys counted
+// in the window or the table with one shared atomic whose result, spread
+// over the run, is every particle's rank among the block's particles of its
+// key (RANK).  A run the table had no room for gets FALLBACK_BIT on its
+// keys; without RANK its count goes straight to the global histogram, with
+// RANK its particles take their slots one by one after the reservations.
+template <bool RANK, int J = 0>
+__device__ __forceinline__ void count_run(const SortArgs &A, SortSmem &S, int k0, SortSizes Z,
+                                          const int (&keys)[SORT_PER_THREAD],
+                                          uint32_t (&rank)[SORT_PER_THREAD], uint32_t &r, bool &fb,
+                                          unsigned &fbmask)
+{
+    const int key = keys[J];
+    if (run_head<J>(keys)) {
+        const int len = run_length<J>(keys);
+        uint32_t b = 0u;
+        fb = false;
+        const unsigned w = (unsigned)(key - k0);
+        if (w < (unsigned)Z.wk) {
+            b = atomicAdd(S.cnt + w, (uint32_t)len);
+        } else {
+            const int slot = hash_insert(S.hkey, key, Z.hb);
+            if (slot >= 0) {
+                b = atomicAdd(S.hcnt + slot, (uint32_t)len);
             } else {
-                const int slot = hash_insert(S.hkey, key, Z.hb);
-                if (slot >= 0)
-                    atomicAdd(S.hcnt + slot, (uint32_t)R.len);
-                else
-                    fb = 1;
+                fb = true;
+                if (!RANK) atomicAdd(A.count + key, (uint32_t)len);
             }
         }
-        const unsigned fbm = __ballot_sync(0xffffffffu, fb);  // heads whose run falls back
-        if (fbm && key >= 0 && ((fbm >> R.hidx) & 1u)) keys[j] = key | FALLBACK_BIT;
-        if (KEEP) runs[j] = pack_run(R);
+        r = b;
+    } else {
+        r += 1u;
     }
+    if (RANK) rank[J] = r;
+    if (fb && key >= 0) fbmask |= 1u << J;  // marked after the walk: the heads compare keys
+    if constexpr (J + 1 < SORT_PER_THREAD)
+        count_run<RANK, J + 1>(A, S, k0, Z, keys, rank, r, fb, fbmask);
+}
+
+template <bool RANK>
+__device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, SortSmem &S,
+                                           int k0, SortSizes Z, int (&keys)[SORT_PER_THREAD],
+                                           uint32_t (&rank)[SORT_PER_THREAD])
+{
+#pragma unroll
+    for (int j = 0; j < SORT_PER_THREAD; ++j)
+        keys[j] = keys[j] == INT_MIN ? -1 : particle_key(G, A.err, keys[j]);
+    uint32_t r = 0u;
+    bool fb = false;
+    unsigned fbmask = 0u;
+    count_run<RANK>(A, S, k0, Z, keys, rank, r, fb, fbmask);
+#pragma unroll
+    for (int j = 0; j < SORT_PER_THREAD; ++j)
+        if (fbmask & (1u << j)) keys[j] |= FALLBACK_BIT;
 }
 
 // Histogram of the keys of particles [base, end) (one sort block).
@@ -280,17 +286,8 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
     const int k0 = window_start(A, G, base, end, Z.wk);
     init_smem(S, Z);
     __syncthreads();
-    int unused[SORT_PER_THREAD];
-    count_keys<false>(A, G, S, base, end, k0, Z, keys, unused);
-#pragma unroll
-    for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
-        // keys the block's table had no room for (rare): counted straight
-        // to the global histogram, one atomic per run
-        if (!__any_sync(0xffffffffu, keys[j] >= 0 && (keys[j] & FALLBACK_BIT))) continue;
-        const Run R = warp_run(keys[j]);
-        if (R.head && keys[j] >= 0 && (keys[j] & FALLBACK_BIT))
-            atomicAdd(A.count + (keys[j] & ~FALLBACK_BIT), (uint32_t)R.len);
-    }
+    uint32_t unused[SORT_PER_THREAD];
+    count_keys<false>(A, G, S, k0, Z, keys, unused);
     __syncthreads();
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
         const uint32_t v = S.cnt[r];
@@ -301,61 +298,44 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
 }
 
 // Shared memory of a scatter block: the counting state with each key's
-// first slot in a block-local staging order, and the global destination of
-// every staged particle.  Once the destinations are known, the staging
-// buffers (up to six fields at a time) take the counting state's place.
-// 56 KB: four blocks fill an SM's 228 KB with their 1 KB reserves.
+// first global slot (gb) and first block-local staging slot (lb), later
+// replaced by the staging records.  A record is one particle's 32 bytes,
+// two 16-byte chunks {cell, ox, oy, vx} {vy, pid, destination, vz}; the
+// second staging pass (the optional extra arrays) reuses the first chunk.
+// 64 KB per block: three blocks per SM.
 struct ScatterCount {
     SortSmem s;
-    uint32_t lbase[SORT_KEYS];
-    uint32_t hlbase[HASH_SLOTS];
-    uint32_t total;
+    uint32_t gb[SORT_KEYS];
+    uint32_t lb[SORT_KEYS];
+    uint32_t hgb[HASH_SLOTS];
+    uint32_t hlb[HASH_SLOTS];
 };
-constexpr int STAGE_FIELDS = 6;
 struct ScatterSmem {
     union {
         ScatterCount c;
-        uint32_t stage[STAGE_FIELDS * SORT_CHUNK];
+        uint4 rec[2 * SORT_CHUNK];
     };
-    uint32_t dst[SORT_CHUNK];
+    uint32_t total;  // particles staged by the block
 };
-static_assert(sizeof(ScatterCount) <= STAGE_FIELDS * SORT_CHUNK * sizeof(uint32_t),
-              "the counting state must fit in the staging buffers");
+static_assert(sizeof(ScatterCount) <= sizeof(uint4) * 2 * SORT_CHUNK,
+              "the counting state must fit in the staging records");
 constexpr size_t SCATTER_SMEM = sizeof(ScatterSmem);
 
-// one staging phase: up to six 32-bit fields moved through shared memory
-// so that the global stores follow the destination order (consecutive
-// threads write consecutive slots of a key's slice); `total` = particles
-// staged by the block
-template <int NF>
-__device__ __forceinline__ void stage_fields(ScatterSmem &S, long long base, long long end,
-                                             const int (&lpos)[SORT_PER_THREAD], int total,
-                                             const uint32_t *const (&src)[NF], uint32_t *const (&dst)[NF])
+// Chunk c of staging record l: record l sits in 128-byte row l >> 2 at
+// chunk position 2 (l & 3) + c, XOR-swizzled by the row so that both the
+// staging writes (lanes' records about eight apart) and the reads (lanes'
+// records consecutive) touch eight distinct chunk positions of a row pair.
+__device__ __forceinline__ uint4 *rec_chunk(uint4 *rec, uint32_t l, int c)
 {
-    static_assert(NF <= STAGE_FIELDS, "staging buffers hold six fields");
-    uint32_t *stage = S.stage;
-    __syncthreads();  // the previous phase (or the counting state) has left the staging buffers
-#pragma unroll
-    for (int j = 0; j < SORT_PER_THREAD; ++j) {
-        const long long i = base + (long long)j * SORT_THREADS + threadIdx.x;
-        if (i < end && lpos[j] >= 0) {
-#pragma unroll
-            for (int f = 0; f < NF; ++f) stage[f * SORT_CHUNK + lpos[j]] = src[f][i];
-        }
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < total; t += SORT_THREADS) {
-        const uint32_t d = S.dst[t];
-        if (d == SORT_NO_SLOT) continue;
-#pragma unroll
-        for (int f = 0; f < NF; ++f) dst[f][d] = stage[f * SORT_CHUNK + t];
-    }
+    const uint32_t row = l >> 2;
+    const uint32_t p = (((l & 3u) << 1) | (uint32_t)c) ^ (((row >> 1) & 7u) ^ (row & 1u));
+    return rec + row * 8u + p;
 }
 
 // Scatter of particles [base, end) (one sort block) to their sorted slots.
 // Each distinct key reserves its global slice (one global atomic per key and
-// block) and a block-local staging range; particles are staged in
-// shared memory in slice order and written out with consecutive threads on
+// block) and a block-local staging range; particles are staged in shared
+// memory in slice order and written out with consecutive threads on
 // consecutive slots.
 __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyGeo &G,
                                                    ScatterSmem &S, long long base, long long end)
@@ -366,81 +346,127 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
     const int k0 = window_start(A, G, base, end, Z.wk);
     ScatterCount &C = S.c;
     init_smem(C.s, Z);
-    if (threadIdx.x == 0) C.total = 0u;
+    if (threadIdx.x == 0) S.total = 0u;
     __syncthreads();
-    int runs[SORT_PER_THREAD];
-    count_keys<true>(A, G, C.s, base, end, k0, Z, keys, runs);
+    uint32_t rank[SORT_PER_THREAD];
+    count_keys<true>(A, G, C.s, k0, Z, keys, rank);
     __syncthreads();
     // reserve each distinct key's slice of the output and of the staging order
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
         const uint32_t v = C.s.cnt[r];
         const bool use = v && k0 + r < A.nkeys;
-        C.s.base[r] = use ? atomicAdd(A.cursor + k0 + r, v) : 0u;
-        C.lbase[r] = use ? atomicAdd(&C.total, v) : 0u;
-        C.s.cnt[r] = 0u;
+        C.gb[r] = use ? atomicAdd(A.cursor + k0 + r, v) : 0u;
+        C.lb[r] = use ? atomicAdd(&S.total, v) : 0u;
     }
     for (int r = threadIdx.x; r < (1 << Z.hb); r += SORT_THREADS) {
         const uint32_t v = C.s.hcnt[r];
-        C.s.hbase[r] = v ? atomicAdd(A.cursor + C.s.hkey[r], v) : 0u;
-        C.hlbase[r] = v ? atomicAdd(&C.total, v) : 0u;
-        C.s.hcnt[r] = 0u;
+        C.hgb[r] = v ? atomicAdd(A.cursor + C.s.hkey[r], v) : 0u;
+        C.hlb[r] = v ? atomicAdd(&S.total, v) : 0u;
     }
     __syncthreads();
-    // destination and staging slot of every particle: one reservation per run
+    // destination and staging slot of every particle
+    uint32_t dst[SORT_PER_THREAD], stg[SORT_PER_THREAD];
 #pragma unroll
-    for (int j = 0; j < SORT_PER_THREAD; ++j) {  // warp-uniform
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
         const int key = keys[j];
-        const Run R = unpack_run(runs[j]);
-        uint32_t d = 0, l = 0;
-        if (R.head && key >= 0) {
-            if (key & FALLBACK_BIT) {
-                d = atomicAdd(A.cursor + (key & ~FALLBACK_BIT), (uint32_t)R.len);
-                l = atomicAdd(&C.total, (uint32_t)R.len);
+        uint32_t d = SORT_NO_SLOT, l = SORT_NO_SLOT;
+        if (key >= 0) {
+            if (key & FALLBACK_BIT) {  // a run the table had no room for (rare)
+                d = atomicAdd(A.cursor + (key & ~FALLBACK_BIT), 1u);
+                l = atomicAdd(&S.total, 1u);
             } else if ((unsigned)(key - k0) < (unsigned)Z.wk) {
-                const int r = key - k0;
-                const uint32_t o = atomicAdd(C.s.cnt + r, (uint32_t)R.len);
-                d = C.s.base[r] + o;
-                l = C.lbase[r] + o;
+                const int w = key - k0;
+                d = C.gb[w] + rank[j];
+                l = C.lb[w] + rank[j];
             } else {
                 const int slot = hash_find(C.s.hkey, key, Z.hb);  // counted in the table in pass 1
-                const uint32_t o = atomicAdd(C.s.hcnt + slot, (uint32_t)R.len);
-                d = C.s.hbase[slot] + o;
-                l = C.hlbase[slot] + o;
+                d = C.hgb[slot] + rank[j];
+                l = C.hlb[slot] + rank[j];
+            }
+            if ((long long)d >= A.nslots) {  // counts that do not match the particles
+                atomicOr(A.err, (unsigned)PIC_DEVERR_SORT);
+                d = SORT_NO_SLOT;
             }
         }
-        d = __shfl_sync(0xffffffffu, d, R.hidx) + (uint32_t)R.rank;
-        l = __shfl_sync(0xffffffffu, l, R.hidx) + (uint32_t)R.rank;
-        if (key >= 0 && (long long)d >= A.nslots) {  // counts that do not match the particles
-            atomicOr(A.err, (unsigned)PIC_DEVERR_SORT);
-            d = SORT_NO_SLOT;
+        dst[j] = d;
+        stg[j] = l;
+    }
+    __syncthreads();  // every thread has read the reservations and taken its slots
+    const uint32_t total = S.total;
+    // stage: the thread's particles (128-bit loads of each field) as records
+    const long long p0 = base + (long long)SORT_PER_THREAD * threadIdx.x;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const long long q = p0 + 4 * h;
+        if (q >= end) continue;  // (not break: the loop must unroll)
+        const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);  // again: an L2 hit
+        const float4 x4 = *reinterpret_cast<const float4 *>(A.oxin + q);
+        const float4 y4 = *reinterpret_cast<const float4 *>(A.oyin + q);
+        const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+        const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+        const uint4 i4 = *reinterpret_cast<const uint4 *>(A.pidin + q);
+        float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (A.vzin) z4 = *reinterpret_cast<const float4 *>(A.vzin + q);
+        const int cs[4] = {c4.x, c4.y, c4.z, c4.w};
+        const float xs[4] = {x4.x, x4.y, x4.z, x4.w}, ys[4] = {y4.x, y4.y, y4.z, y4.w};
+        const float us[4] = {u4.x, u4.y, u4.z, u4.w}, vs[4] = {v4.x, v4.y, v4.z, v4.w};
+        const float zs[4] = {z4.x, z4.y, z4.z, z4.w};
+        const uint32_t is[4] = {i4.x, i4.y, i4.z, i4.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int j = 4 * h + k;
+            if (stg[j] == SORT_NO_SLOT) continue;
+            *rec_chunk(S.rec, stg[j], 0) = make_uint4((uint32_t)cs[k], __float_as_uint(xs[k]),
+                                                      __float_as_uint(ys[k]), __float_as_uint(us[k]));
+            *rec_chunk(S.rec, stg[j], 1) = make_uint4(__float_as_uint(vs[k]), is[k], dst[j],
+                                                      __float_as_uint(zs[k]));
         }
-        if (key >= 0) S.dst[l] = d;
-        keys[j] = key >= 0 ? (int)l : -1;
     }
-    __syncthreads();  // the fallback runs' staging reservations are in
-    const int total = (int)C.total;  // read before the staging buffers overwrite it
-    {
-        const uint32_t *const src[6] = {reinterpret_cast<const uint32_t *>(A.cin),
-                                        reinterpret_cast<const uint32_t *>(A.oxin),
-                                        reinterpret_cast<const uint32_t *>(A.oyin),
-                                        reinterpret_cast<const uint32_t *>(A.vxin),
-                                        reinterpret_cast<const uint32_t *>(A.vyin), A.pidin};
-        uint32_t *const dst[6] = {reinterpret_cast<uint32_t *>(A.cout),
-                                  reinterpret_cast<uint32_t *>(A.oxout),
-                                  reinterpret_cast<uint32_t *>(A.oyout),
-                                  reinterpret_cast<uint32_t *>(A.vxout),
-                                  reinterpret_cast<uint32_t *>(A.vyout), A.pidout};
-        stage_fields<6>(S, base, end, keys, total, src, dst);
+    __syncthreads();
+    // store: consecutive threads take consecutive staged records, so the
+    // stores of one key's slice are consecutive slots
+    for (uint32_t t = threadIdx.x; t < total; t += SORT_THREADS) {
+        const uint4 a = *rec_chunk(S.rec, t, 0);
+        const uint4 b = *rec_chunk(S.rec, t, 1);
+        const uint32_t d = b.z;
+        if (d == SORT_NO_SLOT) continue;
+        A.cout[d] = (int32_t)a.x;
+        A.oxout[d] = __uint_as_float(a.y);
+        A.oyout[d] = __uint_as_float(a.z);
+        A.vxout[d] = __uint_as_float(a.w);
+        A.vyout[d] = __uint_as_float(b.x);
+        A.pidout[d] = b.y;
+        if (A.vzin) A.vzout[d] = __uint_as_float(b.w);
     }
-    if (A.vzin) {
-        const uint32_t *const src[1] = {reinterpret_cast<const uint32_t *>(A.vzin)};
-        uint32_t *const dst[1] = {reinterpret_cast<uint32_t *>(A.vzout)};
-        stage_fields<1>(S, base, end, keys, total, src, dst);
+    if (!A.xin[0]) return;
+    // the four extra arrays, through the first chunk of the same records
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const long long q = p0 + 4 * h;
+        if (q >= end) continue;
+        const uint4 e0 = *reinterpret_cast<const uint4 *>(A.xin[0] + q);
+        const uint4 e1 = *reinterpret_cast<const uint4 *>(A.xin[1] + q);
+        const uint4 e2 = *reinterpret_cast<const uint4 *>(A.xin[2] + q);
+        const uint4 e3 = *reinterpret_cast<const uint4 *>(A.xin[3] + q);
+        const uint32_t a0[4] = {e0.x, e0.y, e0.z, e0.w}, a1[4] = {e1.x, e1.y, e1.z, e1.w};
+        const uint32_t a2[4] = {e2.x, e2.y, e2.z, e2.w}, a3[4] = {e3.x, e3.y, e3.z, e3.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int j = 4 * h + k;
+            if (stg[j] == SORT_NO_SLOT) continue;
+            *rec_chunk(S.rec, stg[j], 0) = make_uint4(a0[k], a1[k], a2[k], a3[k]);
+        }
     }
-    if (A.xin[0]) {
-        const uint32_t *const src[4] = {A.xin[0], A.xin[1], A.xin[2], A.xin[3]};
-        uint32_t *const dst[4] = {A.xout[0], A.xout[1], A.xout[2], A.xout[3]};
-        stage_fields<4>(S, base, end, keys, total, src, dst);
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < total; t += SORT_THREADS) {
+        const uint4 a = *rec_chunk(S.rec, t, 0);
+        const uint32_t d = rec_chunk(S.rec, t, 1)->z;
+        if (d == SORT_NO_SLOT) continue;
+        A.xout[0][d] = a.x;
+        A.xout[1][d] = a.y;
+        A.xout[2][d] = a.z;
+        A.xout[3][d] = a.w;
     }
 }
 
