@@ -791,13 +791,6 @@ def main():
     h.synchronize()
     push_ms = p0.elapsed_time(p1) / reps
     h.poisson()
-    # then one periodic sort on its own (eager, same stream), for the breakdown
-    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s0.record(stream)
-    h.sort()
-    s1.record(stream)
-    h.synchronize()
-    sort_ms = s0.elapsed_time(s1)
     hbm, peak_kind = peaks()
     achieved = BYTES_PER_PARTICLE * N / (push_ms / 1000.0) / 1e9
     step_bytes = BYTES_PER_PARTICLE * N + BYTES_PER_CELL * NX * NY
@@ -854,7 +847,6 @@ def main():
                        "particles": N, "dt": DT, "sort_every": SORT_EVERY,
                        "sorts_in_timed_steps": sorts_timed,
                        "untimed_steps_before": args.warmup + align,
-                       "sort_ms": sort_ms,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (2.7 GB particle arrays per step)",
                        "hbm_frac_step": step_bytes * args.steps / (ms_max / 1000.0) / 1e9 / hbm,

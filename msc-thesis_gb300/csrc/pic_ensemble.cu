@@ -81,7 +81,7 @@ ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun 
     sort_hist_block(A, run_geo(runs[b.run]), S, b.base, b.base + b.count);
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 3)
+__global__ void __launch_bounds__(SORT_THREADS, 4)
 ens_sort_scatter_kernel(SortArgs A, const SegBlock *__restrict__ blk,
                         const EnsRun *__restrict__ runs)
 {

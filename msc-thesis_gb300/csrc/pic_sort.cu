@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
     sort_hist_block(A, single_geo(A), S, base, n);
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 3) sort_scatter_kernel(SortArgs A)
+__global__ void __launch_bounds__(SORT_THREADS, 4) sort_scatter_kernel(SortArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem);

@@ -82,17 +82,16 @@ __device__ __forceinline__ KeyGeo single_geo(const SortArgs &A)
 }
 
 // Work of a sort block: SORT_CHUNK consecutive particles, thread t owning the
-// SORT_PER_THREAD consecutive particles base + 8t ... base + 8t + 7, read
-// with 128-bit loads (base is a multiple of 4 particles, so each half of a
-// thread's eight is 16-byte aligned).
+// quad of four consecutive particles base + 4t ... base + 4t + 3, so that a
+// warp's 128-bit loads are fully coalesced and a warp holds 128 consecutive
+// particles (base is a multiple of 4, so every quad is 16-byte aligned).
 constexpr int SORT_THREADS = 256;
-constexpr int SORT_PER_THREAD = 8;
+constexpr int SORT_PER_THREAD = 4;
 constexpr int SORT_CHUNK = SORT_THREADS * SORT_PER_THREAD;
-constexpr int SORT_KEYS = 2048;
-constexpr int HASH_SLOTS = 1024;  // power of two
+constexpr int SORT_KEYS = 1024;
+constexpr int HASH_SLOTS = 512;  // power of two
 constexpr int HASH_PROBES = 8;
 constexpr int HASH_EMPTY = -1;
-constexpr int FALLBACK_BIT = 1 << 30;  // keys are < 2^30
 constexpr uint32_t SORT_NO_SLOT = 0xFFFFFFFFu;  // a destination outside the slots
 
 // Window and table in use by a sort launch: the arrays are sized for the
@@ -105,7 +104,7 @@ struct SortSizes {
 
 __device__ __forceinline__ SortSizes sort_sizes(const SortArgs &A)
 {
-    return SortSizes{A.wkeys ? A.wkeys : SORT_KEYS, A.hbits ? A.hbits : 10};
+    return SortSizes{A.wkeys ? A.wkeys : SORT_KEYS, A.hbits ? A.hbits : 9};
 }
 
 __device__ __forceinline__ unsigned hash_key(int key, int hb)
@@ -163,8 +162,7 @@ __device__ __forceinline__ int window_start(const SortArgs &A, const KeyGeo &G, 
 }
 
 // Counting state of one sort block: dense window counts and the straggler
-// table.  The scatter keeps, per window key and table slot, the first slot
-// of its global slice (gb) and of its block-local staging range (lb).
+// table.
 struct SortSmem {
     uint32_t cnt[SORT_KEYS];
     int hkey[HASH_SLOTS];
@@ -180,100 +178,132 @@ __device__ __forceinline__ void init_smem(SortSmem &S, SortSizes Z)
     }
 }
 
-// The thread's eight cells (two 128-bit loads); slots at or past `end` get
+// first particle of this thread's quad
+__device__ __forceinline__ long long quad_start(long long base)
+{
+    return base + (long long)SORT_PER_THREAD * threadIdx.x;
+}
+
+// The thread's quad of cells (one 128-bit load); slots at or past `end` get
 // INT_MIN (no particle).
 __device__ __forceinline__ void load_cells(const SortArgs &A, long long base, long long end,
                                            int (&cells)[SORT_PER_THREAD])
 {
-    const long long p0 = base + (long long)SORT_PER_THREAD * threadIdx.x;
+    const long long q = quad_start(base);
+    int4 c = make_int4(INT_MIN, INT_MIN, INT_MIN, INT_MIN);
+    if (q < end) c = *reinterpret_cast<const int4 *>(A.cin + q);
+    cells[0] = c.x;
+    cells[1] = q + 1 < end ? c.y : INT_MIN;
+    cells[2] = q + 2 < end ? c.z : INT_MIN;
+    cells[3] = q + 3 < end ? c.w : INT_MIN;
+}
+
+// Runs of equal keys over the warp's 128 consecutive particles (lane l holds
+// positions 4l .. 4l + 3), from shuffles and ballots: every run is counted
+// by the lane holding its first particle, with its full length, so that a
+// run costs one atomic whatever the lanes it spans.
+struct QuadRuns {
+    unsigned head;  // bit j: particle j starts a run
+    int len[SORT_PER_THREAD];  // run length at each head
+    int lin;        // lane holding the head of the run that enters this lane
+    int pin;        // that head's position in the warp (0..127)
+};
+
+__device__ __forceinline__ QuadRuns quad_runs(const int (&k)[SORT_PER_THREAD])
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(full, k[3], 1);
+    QuadRuns R;
+    R.head = (lane == 0 || k[0] != prev ? 1u : 0u) | (k[1] != k[0] ? 2u : 0u) |
+             (k[2] != k[1] ? 4u : 0u) | (k[3] != k[2] ? 8u : 0u);
+    const unsigned lanes = __ballot_sync(full, R.head != 0u);  // lanes holding a head (lane 0 does)
+    const int firstj = __ffs(R.head) - 1;                       // -1: no head
+    const int lastj = 31 - __clz(R.head);                       // -1: no head
+    // first head after this lane: its position, or 128
+    const unsigned later = lanes & ~(0xffffffffu >> (31 - lane));
+    const int fl = later ? __ffs(later) - 1 : 0;
+    const int ffj = __shfl_sync(full, firstj, fl);
+    const int next_pos = later ? 4 * fl + ffj : 4 * 32;
+    // the run holding this lane's first particle, when it starts in an
+    // earlier lane: at the last head of the nearest earlier lane with one
+    const unsigned before = lanes & ((1u << lane) - 1u);
+    R.lin = before ? 31 - __clz(before) : 0;
+    R.pin = 4 * R.lin + __shfl_sync(full, lastj, R.lin);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const long long q = p0 + 4 * h;
-        int4 c = make_int4(INT_MIN, INT_MIN, INT_MIN, INT_MIN);
-        if (q < end) c = *reinterpret_cast<const int4 *>(A.cin + q);
-        cells[4 * h + 0] = c.x;
-        cells[4 * h + 1] = q + 1 < end ? c.y : INT_MIN;
-        cells[4 * h + 2] = q + 2 < end ? c.z : INT_MIN;
-        cells[4 * h + 3] = q + 3 < end ? c.w : INT_MIN;
-    }
-}
-
-// Length of the run of equal keys that starts at particle j of the thread's
-// eight consecutive particles (compile-time indices only).
-template <int J>
-__device__ __forceinline__ int run_length(const int (&keys)[SORT_PER_THREAD])
-{
-    int l = 1;
-    bool same = true;
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        int nxt = next_pos;
 #pragma unroll
-    for (int k = J + 1; k < SORT_PER_THREAD; ++k) {
-        same = same && keys[k] == keys[J];
-        l += same ? 1 : 0;
+        for (int i = SORT_PER_THREAD - 1; i > j; --i)
+            if (R.head & (1u << i)) nxt = 4 * lane + i;
+        R.len[j] = nxt - (4 * lane + j);
     }
-    return l;
+    return R;
 }
 
-template <int J>
-__device__ __forceinline__ bool run_head(const int (&keys)[SORT_PER_THREAD])
-{
-    return keys[J] >= 0 && (J == 0 || keys[J] != keys[J > 0 ? J - 1 : 0]);
-}
-
-// Pass 1 of both kernels: the keys of the thread's particles (`keys` holds
-// their cells on entry; INT_MIN becomes -1), each run of equal keys counted
-// in the window or the table with one shared atomic whose result, spread
-// over the run, is every particle's rank among the block's particles of its
-// key (RANK).  A run the table had no room for gets FALLBACK_BIT on its
-// keys; without RANK its count goes straight to the global histogram, with
-// RANK its particles take their slots one by one after the reservations.
-template <bool RANK, int J = 0>
-__device__ __forceinline__ void count_run(const SortArgs &A, SortSmem &S, int k0, SortSizes Z,
-                                          const int (&keys)[SORT_PER_THREAD],
-                                          uint32_t (&rank)[SORT_PER_THREAD], uint32_t &r, bool &fb,
-                                          unsigned &fbmask)
-{
-    const int key = keys[J];
-    if (run_head<J>(keys)) {
-        const int len = run_length<J>(keys);
-        uint32_t b = 0u;
-        fb = false;
-        const unsigned w = (unsigned)(key - k0);
-        if (w < (unsigned)Z.wk) {
-            b = atomicAdd(S.cnt + w, (uint32_t)len);
-        } else {
-            const int slot = hash_insert(S.hkey, key, Z.hb);
-            if (slot >= 0) {
-                b = atomicAdd(S.hcnt + slot, (uint32_t)len);
-            } else {
-                fb = true;
-                if (!RANK) atomicAdd(A.count + key, (uint32_t)len);
-            }
-        }
-        r = b;
-    } else {
-        r += 1u;
-    }
-    if (RANK) rank[J] = r;
-    if (fb && key >= 0) fbmask |= 1u << J;  // marked after the walk: the heads compare keys
-    if constexpr (J + 1 < SORT_PER_THREAD)
-        count_run<RANK, J + 1>(A, S, k0, Z, keys, rank, r, fb, fbmask);
-}
-
+// Pass 1 of both kernels: the keys of the thread's quad (`keys` holds its
+// cells on entry; INT_MIN becomes -1) and one shared atomic per run of equal
+// keys (quad_runs), in the window or the table.  With RANK every particle
+// gets its rank among the block's particles of its key: the run's atomic
+// result plus its position in the run.  A run the table has no room for
+// falls back: without RANK its count goes straight to the global histogram,
+// with RANK its particles are marked in `fbm` and take their slots one by
+// one after the reservations.
 template <bool RANK>
 __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, SortSmem &S,
                                            int k0, SortSizes Z, int (&keys)[SORT_PER_THREAD],
-                                           uint32_t (&rank)[SORT_PER_THREAD])
+                                           uint32_t (&rank)[SORT_PER_THREAD], unsigned &fbm)
 {
 #pragma unroll
     for (int j = 0; j < SORT_PER_THREAD; ++j)
         keys[j] = keys[j] == INT_MIN ? -1 : particle_key(G, A.err, keys[j]);
-    uint32_t r = 0u;
-    bool fb = false;
-    unsigned fbmask = 0u;
-    count_run<RANK>(A, S, k0, Z, keys, rank, r, fb, fbmask);
+    const QuadRuns R = quad_runs(keys);
+    uint32_t base[SORT_PER_THREAD];
+    bool fbh[SORT_PER_THREAD];
 #pragma unroll
-    for (int j = 0; j < SORT_PER_THREAD; ++j)
-        if (fbmask & (1u << j)) keys[j] |= FALLBACK_BIT;
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        base[j] = 0u;
+        fbh[j] = false;
+        const int key = keys[j];
+        if (((R.head >> j) & 1u) && key >= 0) {
+            const unsigned w = (unsigned)(key - k0);
+            if (w < (unsigned)Z.wk) {
+                base[j] = atomicAdd(S.cnt + w, (uint32_t)R.len[j]);
+            } else {
+                const int slot = hash_insert(S.hkey, key, Z.hb);
+                if (slot >= 0) {
+                    base[j] = atomicAdd(S.hcnt + slot, (uint32_t)R.len[j]);
+                } else {
+                    fbh[j] = true;
+                    if (!RANK) atomicAdd(A.count + key, (uint32_t)R.len[j]);
+                }
+            }
+        }
+    }
+    fbm = 0u;
+    if (!RANK) return;
+    // the run entering this lane takes its base and fallback flag from the
+    // lane holding its head (that lane's last head)
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned hb = R.head;
+    const uint32_t lastbase = (hb & 8u) ? base[3] : (hb & 4u) ? base[2] : (hb & 2u) ? base[1] : base[0];
+    const bool lastfb = (hb & 8u) ? fbh[3] : (hb & 4u) ? fbh[2] : (hb & 2u) ? fbh[1] : fbh[0];
+    const uint32_t in_base = __shfl_sync(full, lastbase, R.lin);
+    const bool in_fb = __shfl_sync(full, lastfb ? 1 : 0, R.lin) != 0;
+    uint32_t r = in_base + (uint32_t)(4 * lane - R.pin);
+    bool fb = in_fb;
+#pragma unroll
+    for (int j = 0; j < SORT_PER_THREAD; ++j) {
+        if ((hb >> j) & 1u) {
+            r = base[j];
+            fb = fbh[j];
+        } else if (j > 0) {
+            r += 1u;
+        }
+        rank[j] = r;
+        if (fb && keys[j] >= 0) fbm |= 1u << j;
+    }
 }
 
 // Histogram of the keys of particles [base, end) (one sort block).
@@ -287,7 +317,8 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
     init_smem(S, Z);
     __syncthreads();
     uint32_t unused[SORT_PER_THREAD];
-    count_keys<false>(A, G, S, k0, Z, keys, unused);
+    unsigned fbm;
+    count_keys<false>(A, G, S, k0, Z, keys, unused, fbm);
     __syncthreads();
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
         const uint32_t v = S.cnt[r];
@@ -302,7 +333,6 @@ __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo 
 // replaced by the staging records.  A record is one particle's 32 bytes,
 // two 16-byte chunks {cell, ox, oy, vx} {vy, pid, destination, vz}; the
 // second staging pass (the optional extra arrays) reuses the first chunk.
-// 64 KB per block: three blocks per SM.
 struct ScatterCount {
     SortSmem s;
     uint32_t gb[SORT_KEYS];
@@ -322,34 +352,51 @@ static_assert(sizeof(ScatterCount) <= sizeof(uint4) * 2 * SORT_CHUNK,
 constexpr size_t SCATTER_SMEM = sizeof(ScatterSmem);
 
 // Chunk c of staging record l: record l sits in 128-byte row l >> 2 at
-// chunk position 2 (l & 3) + c, XOR-swizzled by the row so that both the
-// staging writes (lanes' records about eight apart) and the reads (lanes'
-// records consecutive) touch eight distinct chunk positions of a row pair.
+// chunk position 2 (l & 3) + c, XOR-swizzled by the row's low three bits.
+// Eight lanes whose records are four apart (particles four apart in one
+// cell) then write eight rows at eight distinct positions, and eight lanes
+// reading consecutive records read two rows at positions of opposite
+// parity: no bank conflicts either way.
 __device__ __forceinline__ uint4 *rec_chunk(uint4 *rec, uint32_t l, int c)
 {
     const uint32_t row = l >> 2;
-    const uint32_t p = (((l & 3u) << 1) | (uint32_t)c) ^ (((row >> 1) & 7u) ^ (row & 1u));
+    const uint32_t p = (((l & 3u) << 1) | (uint32_t)c) ^ (row & 7u);
     return rec + row * 8u + p;
 }
 
 // Scatter of particles [base, end) (one sort block) to their sorted slots.
-// Each distinct key reserves its global slice (one global atomic per key and
-// block) and a block-local staging range; particles are staged in shared
-// memory in slice order and written out with consecutive threads on
-// consecutive slots.
+// Every field of the thread's quad is loaded first, so that those loads'
+// latency overlaps the counting.  Each distinct key reserves its global
+// slice (one global atomic per key and block) and a block-local staging
+// range; the particles are staged in shared memory in slice order and
+// written out with consecutive threads on consecutive slots.
 __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyGeo &G,
                                                    ScatterSmem &S, long long base, long long end)
 {
     const SortSizes Z = sort_sizes(A);
+    const long long q = quad_start(base);
+    const bool live = q < end;
     int keys[SORT_PER_THREAD];
     load_cells(A, base, end, keys);
+    const int cs[SORT_PER_THREAD] = {keys[0], keys[1], keys[2], keys[3]};
+    float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f), y4 = x4, u4 = x4, v4 = x4, z4 = x4;
+    uint4 i4 = make_uint4(0u, 0u, 0u, 0u);
+    if (live) {
+        x4 = *reinterpret_cast<const float4 *>(A.oxin + q);
+        y4 = *reinterpret_cast<const float4 *>(A.oyin + q);
+        u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
+        v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
+        i4 = *reinterpret_cast<const uint4 *>(A.pidin + q);
+        if (A.vzin) z4 = *reinterpret_cast<const float4 *>(A.vzin + q);
+    }
     const int k0 = window_start(A, G, base, end, Z.wk);
     ScatterCount &C = S.c;
     init_smem(C.s, Z);
     if (threadIdx.x == 0) S.total = 0u;
     __syncthreads();
     uint32_t rank[SORT_PER_THREAD];
-    count_keys<true>(A, G, C.s, k0, Z, keys, rank);
+    unsigned fbm;
+    count_keys<true>(A, G, C.s, k0, Z, keys, rank, fbm);
     __syncthreads();
     // reserve each distinct key's slice of the output and of the staging order
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
@@ -371,8 +418,8 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
         const int key = keys[j];
         uint32_t d = SORT_NO_SLOT, l = SORT_NO_SLOT;
         if (key >= 0) {
-            if (key & FALLBACK_BIT) {  // a run the table had no room for (rare)
-                d = atomicAdd(A.cursor + (key & ~FALLBACK_BIT), 1u);
+            if (fbm & (1u << j)) {  // a run the table had no room for (rare)
+                d = atomicAdd(A.cursor + key, 1u);
                 l = atomicAdd(&S.total, 1u);
             } else if ((unsigned)(key - k0) < (unsigned)Z.wk) {
                 const int w = key - k0;
@@ -393,33 +440,18 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
     }
     __syncthreads();  // every thread has read the reservations and taken its slots
     const uint32_t total = S.total;
-    // stage: the thread's particles (128-bit loads of each field) as records
-    const long long p0 = base + (long long)SORT_PER_THREAD * threadIdx.x;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const long long q = p0 + 4 * h;
-        if (q >= end) continue;  // (not break: the loop must unroll)
-        const int4 c4 = *reinterpret_cast<const int4 *>(A.cin + q);  // again: an L2 hit
-        const float4 x4 = *reinterpret_cast<const float4 *>(A.oxin + q);
-        const float4 y4 = *reinterpret_cast<const float4 *>(A.oyin + q);
-        const float4 u4 = *reinterpret_cast<const float4 *>(A.vxin + q);
-        const float4 v4 = *reinterpret_cast<const float4 *>(A.vyin + q);
-        const uint4 i4 = *reinterpret_cast<const uint4 *>(A.pidin + q);
-        float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (A.vzin) z4 = *reinterpret_cast<const float4 *>(A.vzin + q);
-        const int cs[4] = {c4.x, c4.y, c4.z, c4.w};
+    {
         const float xs[4] = {x4.x, x4.y, x4.z, x4.w}, ys[4] = {y4.x, y4.y, y4.z, y4.w};
         const float us[4] = {u4.x, u4.y, u4.z, u4.w}, vs[4] = {v4.x, v4.y, v4.z, v4.w};
         const float zs[4] = {z4.x, z4.y, z4.z, z4.w};
         const uint32_t is[4] = {i4.x, i4.y, i4.z, i4.w};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int j = 4 * h + k;
+        for (int j = 0; j < SORT_PER_THREAD; ++j) {
             if (stg[j] == SORT_NO_SLOT) continue;
-            *rec_chunk(S.rec, stg[j], 0) = make_uint4((uint32_t)cs[k], __float_as_uint(xs[k]),
-                                                      __float_as_uint(ys[k]), __float_as_uint(us[k]));
-            *rec_chunk(S.rec, stg[j], 1) = make_uint4(__float_as_uint(vs[k]), is[k], dst[j],
-                                                      __float_as_uint(zs[k]));
+            *rec_chunk(S.rec, stg[j], 0) = make_uint4((uint32_t)cs[j], __float_as_uint(xs[j]),
+                                                      __float_as_uint(ys[j]), __float_as_uint(us[j]));
+            *rec_chunk(S.rec, stg[j], 1) = make_uint4(__float_as_uint(vs[j]), is[j], dst[j],
+                                                      __float_as_uint(zs[j]));
         }
     }
     __syncthreads();
@@ -441,10 +473,7 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
     if (!A.xin[0]) return;
     // the four extra arrays, through the first chunk of the same records
     __syncthreads();
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const long long q = p0 + 4 * h;
-        if (q >= end) continue;
+    if (live) {
         const uint4 e0 = *reinterpret_cast<const uint4 *>(A.xin[0] + q);
         const uint4 e1 = *reinterpret_cast<const uint4 *>(A.xin[1] + q);
         const uint4 e2 = *reinterpret_cast<const uint4 *>(A.xin[2] + q);
@@ -452,10 +481,9 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
         const uint32_t a0[4] = {e0.x, e0.y, e0.z, e0.w}, a1[4] = {e1.x, e1.y, e1.z, e1.w};
         const uint32_t a2[4] = {e2.x, e2.y, e2.z, e2.w}, a3[4] = {e3.x, e3.y, e3.z, e3.w};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int j = 4 * h + k;
+        for (int j = 0; j < SORT_PER_THREAD; ++j) {
             if (stg[j] == SORT_NO_SLOT) continue;
-            *rec_chunk(S.rec, stg[j], 0) = make_uint4(a0[k], a1[k], a2[k], a3[k]);
+            *rec_chunk(S.rec, stg[j], 0) = make_uint4(a0[j], a1[j], a2[j], a3[j]);
         }
     }
     __syncthreads();
