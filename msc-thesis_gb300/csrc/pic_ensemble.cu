@@ -68,9 +68,9 @@ ens_push_kernel(PushArgs A, const SegBlock *__restrict__ blk, const EnsRun *__re
     push_block<GATHER, DEPOSIT, false>(A, G, smem, b.base, b.base + b.count, anchor[blockIdx.x]);
 }
 
-__device__ __forceinline__ KeyGeo run_geo(const EnsRun &R)
+__device__ __forceinline__ KeyGeo run_geo(const EnsRun &R, int rows)
 {
-    return key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off);
+    return key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off, rows);
 }
 
 __global__ void __launch_bounds__(SORT_THREADS)
@@ -78,7 +78,7 @@ ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun 
 {
     __shared__ SortSmem S;
     const SegBlock b = blk[blockIdx.x];
-    sort_hist_block(A, run_geo(runs[b.run]), S, b.base, b.base + b.count);
+    sort_hist_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
 }
 
 __global__ void __launch_bounds__(SORT_THREADS, 4)
@@ -88,7 +88,7 @@ ens_sort_scatter_kernel(SortArgs A, const SegBlock *__restrict__ blk,
     extern __shared__ __align__(16) unsigned char smem[];
     ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem);
     const SegBlock b = blk[blockIdx.x];
-    sort_scatter_block(A, run_geo(runs[b.run]), S, b.base, b.base + b.count);
+    sort_scatter_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
 }
 
 // tile of the first particle of every push block, from the sorted buffer
@@ -498,9 +498,11 @@ SortArgs ens_sort_args(pic_ensemble *E, const float *const *xin, float *const *x
     A.nkeys = E->nkeys;
     A.nslots = E->nslots;
     A.err = &E->dev[0].err;
-    double density = 1e30;  // the sparsest run sizes the window
+    // keys are tile rows; the sparsest run (particles per row) sizes the window
+    A.rows = 1;
+    double density = 1e30;
     for (const EnsRun &R : E->runs)
-        if (R.n) density = std::min(density, (double)R.n / ((double)R.nx * R.ny));
+        if (R.n) density = std::min(density, (double)R.n * R.tw / ((double)R.nx * R.ny));
     sort_sizes_for(density, &A.wkeys, &A.hbits);
     for (int k = 0; k < 4; ++k) {
         A.xin[k] = xin ? reinterpret_cast<const uint32_t *>(xin[k]) : nullptr;

@@ -283,7 +283,10 @@ static SortArgs sort_args(pic_handle *h, int s)
     A.err = &h->dev->err;
     A.nkeys = ncell + 1;  // cells + the bin of empty slots
     A.nslots = B.cap;
-    sort_sizes_for((double)B.n / (double)ncell, &A.wkeys, &A.hbits);
+    // the DSMC species is sorted by cell (its pass pairs particles per cell);
+    // every other species by tile row (keys 0 .. ncell / tw - 1 of the same space)
+    A.rows = (h->dsmc.on && s == h->dsmc.s) ? 0 : 1;
+    sort_sizes_for((double)B.n / (double)ncell * (A.rows ? g.tw : 1), &A.wkeys, &A.hbits);
     return A;
 }
 

@@ -32,6 +32,7 @@ struct SortArgs {
     int nx, ny, tw, th, ntx, chunk;
     long long nkeys;  // keys of the whole key space (cells + empty bins)
     unsigned int *err;
+    int rows;                // sort by tile row (tw cells per key) instead of by cell
     const uint32_t *xin[4];  // optional extra per-particle arrays moved along
     uint32_t *xout[4];       // (all four or none)
     int wkeys, hbits;        // window keys and log2 hash slots in use (0: the maxima)
@@ -41,10 +42,12 @@ struct SortArgs {
 // Key geometry of the run a sort block works on: the run's grid and tiles
 // and the first key of its range (0 for a single run).  Key key_off + nx*ny
 // is the run's bin of empty slots.  mtw, mth: multipliers that divide a
-// cell coordinate by tw and th (div_coord); 0 divides directly.
+// cell coordinate by tw and th (div_coord); 0 divides directly.  rows: keys
+// are tile rows (tw cells each) rather than cells.
 struct KeyGeo {
     int nx, ny, tw, th, ntx, key_off;
     unsigned mtw, mth;
+    int rows;
 };
 
 // m = floor((2^32 - 1) / d) + 1 gives floor(n / d) = umulhi(n, m) for every
@@ -57,9 +60,9 @@ __host__ __device__ __forceinline__ unsigned div_magic(int d)
 }
 
 __host__ __device__ __forceinline__ KeyGeo key_geo(int nx, int ny, int tw, int th, int ntx,
-                                                   int key_off)
+                                                   int key_off, int rows = 0)
 {
-    return KeyGeo{nx, ny, tw, th, ntx, key_off, div_magic(tw), div_magic(th)};
+    return KeyGeo{nx, ny, tw, th, ntx, key_off, div_magic(tw), div_magic(th), rows};
 }
 
 __device__ __forceinline__ int div_coord(int n, int d, unsigned m)
@@ -76,9 +79,22 @@ __device__ __forceinline__ int cell_key(int c, const KeyGeo &G)
     return ((ty * G.ntx + tx) * G.th + ly) * G.tw + lx;
 }
 
+// Sort key of an on-grid cell c: its tile-major cell index, or with G.rows
+// the tile-major index of its row within its tile (cell index / tw).  The
+// push only needs a block's particles to stay within its tiles, and
+// measured no slower on row-sorted particles; the DSMC pass needs cells.
+__device__ __forceinline__ int sort_key(int c, const KeyGeo &G)
+{
+    const int cx = c & 0xFFFF, cy = c >> 16;
+    const int tx = div_coord(cx, G.tw, G.mtw);
+    const int ty = div_coord(cy, G.th, G.mth), ly = cy - ty * G.th;
+    const int row = (ty * G.ntx + tx) * G.th + ly;
+    return G.rows ? row : row * G.tw + (cx - tx * G.tw);
+}
+
 __device__ __forceinline__ KeyGeo single_geo(const SortArgs &A)
 {
-    return key_geo(A.nx, A.ny, A.tw, A.th, A.ntx, 0);
+    return key_geo(A.nx, A.ny, A.tw, A.th, A.ntx, 0, A.rows);
 }
 
 // Work of a sort block: SORT_CHUNK consecutive particles, thread t owning the
@@ -147,7 +163,7 @@ __device__ __forceinline__ int particle_key(const KeyGeo &G, unsigned int *err, 
         atomicOr(err, (unsigned)PIC_DEVERR_CELL);
         return empty;
     }
-    return G.key_off + cell_key(c, G);
+    return G.key_off + sort_key(c, G);
 }
 
 // first key of this block's shared-memory window (block-uniform)
@@ -157,7 +173,7 @@ __device__ __forceinline__ int window_start(const SortArgs &A, const KeyGeo &G, 
     const long long mid = min(base + SORT_CHUNK / 2, end - 1);
     const int c = A.cin[mid];
     int k = G.key_off;
-    if (c >= 0 && (c & 0xFFFF) < G.nx && (c >> 16) < G.ny) k += cell_key(c, G);
+    if (c >= 0 && (c & 0xFFFF) < G.nx && (c >> 16) < G.ny) k += sort_key(c, G);
     return max(0, k - wk / 2);
 }
 
