@@ -38,13 +38,15 @@
 
 namespace pic {
 
+constexpr int HIST_SUB = 4;  // sort chunks per histogram block of a single run
+
 __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
 {
     __shared__ SortSmem S;
     const long long n = *A.d_n;
-    const long long base = (long long)blockIdx.x * SORT_CHUNK;
+    const long long base = (long long)blockIdx.x * (HIST_SUB * SORT_CHUNK);
     if (base >= n) return;
-    sort_hist_block(A, single_geo(A), S, base, n);
+    sort_hist_block<HIST_SUB>(A, single_geo(A), S, base, n);
 }
 
 __global__ void __launch_bounds__(SORT_THREADS, 4) sort_scatter_kernel(SortArgs A)
@@ -295,7 +297,8 @@ static pic_status launch_hist(pic_handle *h, int s, const SortArgs &A)
 {
     const SpeciesBuf &B = h->sp[s];
     PIC_CUDA(cudaMemsetAsync(A.count, 0, sizeof(uint32_t) * (size_t)A.nkeys, h->stream));
-    sort_hist_kernel<<<(unsigned)((B.cap + SORT_CHUNK - 1) / SORT_CHUNK), SORT_THREADS, 0, h->stream>>>(A);
+    const long long hc = (long long)HIST_SUB * SORT_CHUNK;
+    sort_hist_kernel<<<(unsigned)((B.cap + hc - 1) / hc), SORT_THREADS, 0, h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }

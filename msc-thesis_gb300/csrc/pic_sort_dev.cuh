@@ -166,11 +166,12 @@ __device__ __forceinline__ int particle_key(const KeyGeo &G, unsigned int *err, 
     return G.key_off + sort_key(c, G);
 }
 
-// first key of this block's shared-memory window (block-uniform)
+// first key of the shared-memory window of a block over particles
+// [base, end) (block-uniform): centred on the middle particle's key
 __device__ __forceinline__ int window_start(const SortArgs &A, const KeyGeo &G, long long base,
                                             long long end, int wk)
 {
-    const long long mid = min(base + SORT_CHUNK / 2, end - 1);
+    const long long mid = base + (end - base - 1) / 2;
     const int c = A.cin[mid];
     int k = G.key_off;
     if (c >= 0 && (c & 0xFFFF) < G.nx && (c >> 16) < G.ny) k += sort_key(c, G);
@@ -322,19 +323,25 @@ __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, S
     }
 }
 
-// Histogram of the keys of particles [base, end) (one sort block).
+// Histogram of the keys of particles [base, end) (one sort block of SUB
+// consecutive SORT_CHUNK-particle sub-chunks: every quad's cells are loaded
+// before the first is counted, so that one block keeps SUB loads per
+// thread in flight and pays its barriers and window once).
+template <int SUB = 1>
 __device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo &G, SortSmem &S,
                                                 long long base, long long end)
 {
     const SortSizes Z = sort_sizes(A);
-    int keys[SORT_PER_THREAD];
-    load_cells(A, base, end, keys);
-    const int k0 = window_start(A, G, base, end, Z.wk);
+    int keys[SUB][SORT_PER_THREAD];
+#pragma unroll
+    for (int u = 0; u < SUB; ++u) load_cells(A, base + (long long)u * SORT_CHUNK, end, keys[u]);
+    const int k0 = window_start(A, G, base, min(end, base + (long long)SUB * SORT_CHUNK), Z.wk);
     init_smem(S, Z);
     __syncthreads();
     uint32_t unused[SORT_PER_THREAD];
     unsigned fbm;
-    count_keys<false>(A, G, S, k0, Z, keys, unused, fbm);
+#pragma unroll
+    for (int u = 0; u < SUB; ++u) count_keys<false>(A, G, S, k0, Z, keys[u], unused, fbm);
     __syncthreads();
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
         const uint32_t v = S.cnt[r];
@@ -405,7 +412,7 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
         i4 = *reinterpret_cast<const uint4 *>(A.pidin + q);
         if (A.vzin) z4 = *reinterpret_cast<const float4 *>(A.vzin + q);
     }
-    const int k0 = window_start(A, G, base, end, Z.wk);
+    const int k0 = window_start(A, G, base, min(end, base + (long long)SORT_CHUNK), Z.wk);
     ScatterCount &C = S.c;
     init_smem(C.s, Z);
     if (threadIdx.x == 0) S.total = 0u;
