@@ -25,6 +25,15 @@ __device__ __forceinline__ Cic4 cic_weights(unsigned cnt, unsigned sfx, unsigned
     return W;
 }
 
+// rint(o 2^16) for an in-cell offset o in [0, 1), round to nearest even:
+// adding 1.5 2^23 in the same fused operation leaves the rounded integer in
+// the low mantissa bits (one rounding of the exact o 2^16 + 1.5 2^23, whose
+// unit in the last place is 1), the same value as __float2uint_rn(o * 65536)
+__device__ __forceinline__ unsigned offset_fixed(float o)
+{
+    return __float_as_uint(fmaf(o, 65536.0f, 12582912.0f)) - 0x4B400000u;
+}
+
 __device__ __forceinline__ void deposit_global(unsigned long long *rho, int nx, int ny, int cx,
                                                int cy, const Cic4 &W, unsigned long long q)
 {
@@ -154,18 +163,31 @@ __device__ __forceinline__ void load_window(const PushGeo &A, const Window &W)
         for (int i = threadIdx.x; i < 5 * W.nc; i += blockDim.x) W.sM[i] = 0u;
 }
 
-// One group of `cnt` particles in one cell with sums fx, fy, fx*fy: its
-// moments added to the window's cell (five shared atomics; the node weights
-// are linear in them and are formed at the flush), or its node weights
-// straight to the grid outside the window.
-__device__ __forceinline__ void deposit_group(const PushGeo &A, const Window &W, int cx, int cy,
-                                              unsigned cnt, unsigned sfx, unsigned sfy,
-                                              unsigned long long sxy)
+// Window coordinates of cell (cx, cy): its column and row counted from the
+// window's first (periodically), so that it lies in the window exactly
+// when 0 <= dxl < wcx and 0 <= dyl < wcy.
+__device__ __forceinline__ void window_coords(const PushGeo &A, const Window &W, int cx, int cy,
+                                              int &dxl, int &dyl)
 {
-    int dxl = cx - W.wx0, dyl = cy - W.wy0;
+    dxl = cx - W.wx0;
+    dyl = cy - W.wy0;
     if (dxl < 0) dxl += A.nx;
     if (dyl < 0) dyl += A.ny;
-    if (W.on && dxl < A.wcx && dyl < A.wcy) {
+}
+
+// One group of `cnt` particles in cell (cx, cy), window coordinates (dxl,
+// dyl), with sums fx, fy, fx*fy: its moments added to the window's cell
+// (five shared atomics; the node weights are linear in them and are formed
+// at the flush), or its node weights straight to the grid outside the
+// window.  The window coordinates may run one carry past the range of
+// window_coords (a column or row from -1 to nx): any value maps to the
+// grid node the flush gives it, and values outside [0, wcx) x [0, wcy)
+// take the grid path.
+__device__ __forceinline__ void deposit_group(const PushGeo &A, const Window &W, int cx, int cy,
+                                              int dxl, int dyl, unsigned cnt, unsigned sfx,
+                                              unsigned sfy, unsigned long long sxy)
+{
+    if (W.on && (unsigned)dxl < (unsigned)A.wcx && (unsigned)dyl < (unsigned)A.wcy) {
         unsigned *m = W.sM + dyl * A.wcx + dxl;
         atomicAdd(m, cnt);
         atomicAdd(m + W.nc, sfx);
@@ -225,7 +247,7 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
     // register aggregate of the particles that share the first one's new cell
     unsigned gcnt = 0u, gfx = 0u, gfy = 0u;
     unsigned long long gxy = 0ull;
-    int gkey = -1, gcx = 0, gcy = 0;
+    int gkey = -1, gdx = 0, gdy = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int c = cc[j];
@@ -237,13 +259,12 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
             continue;
         }
         float ox = xo[j], oy = yo[j], vx = xv[j], vy = yv[j];
+        int dxl, dyl;  // window coordinates, advanced with the cell below
+        window_coords(A, W, cx, cy, dxl, dyl);
         if (!MOVE) {
         } else if (GATHER) {
             const float gx = 1.f - ox, gy = 1.f - oy;
             float2 e00, e10, e01, e11;
-            int dxl = cx - W.wx0, dyl = cy - W.wy0;
-            if (dxl < 0) dxl += nx;
-            if (dyl < 0) dyl += ny;
             if (W.on && dxl < A.wcx && dyl < A.wcy) {
                 const int i = dyl * W.nwx + dxl;
                 e00 = W.sE[i];
@@ -274,8 +295,8 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
             py = fmaf(2.f, vy, py);
         }
         if (MOVE) {
-            bad |= !(fabsf(vx) <= 3.0e38f) || !(fabsf(vy) <= 3.0e38f);
-            // drift in cell units; carry whole cells into the index
+            // drift in cell units; carry whole cells into the index (a
+            // non-finite velocity shows in the thread's kinetic-energy sum)
             ox = fmaf(vx, A.dtdx, ox);
             oy = fmaf(vy, A.dtdy, oy);
             float sx = floorf(ox), sy = floorf(oy);
@@ -283,8 +304,11 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
             oy -= sy;
             if (ox >= 1.f) { ox -= 1.f; sx += 1.f; }
             if (oy >= 1.f) { oy -= 1.f; sy += 1.f; }
-            cx += (int)sx;
-            cy += (int)sy;
+            const int kx = (int)sx, ky = (int)sy;
+            cx += kx;
+            cy += ky;
+            dxl += kx;
+            dyl += ky;
             if ((unsigned)cx >= (unsigned)nx) { cx %= nx; if (cx < 0) cx += nx; }
             if ((unsigned)cy >= (unsigned)ny) { cy %= ny; if (cy < 0) cy += ny; }
         }
@@ -299,13 +323,12 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
         xv[j] = vx;
         yv[j] = vy;
         if (DEPOSIT) {
-            const unsigned fx = __float2uint_rn(ox * 65536.0f);
-            const unsigned fy = __float2uint_rn(oy * 65536.0f);
+            const unsigned fx = offset_fixed(ox), fy = offset_fixed(oy);
             const unsigned long long fxy = (unsigned long long)fx * fy;
             if (gkey < 0) {
                 gkey = cn;
-                gcx = cx;
-                gcy = cy;
+                gdx = dxl;
+                gdy = dyl;
             }
             if (cn == gkey) {
                 ++gcnt;
@@ -313,15 +336,15 @@ __device__ __forceinline__ void push_quad(const PushGeo &A, const Window &W, int
                 gfy += fy;
                 gxy += fxy;
             } else {
-                deposit_group(A, W, cx, cy, 1u, fx, fy, fxy);
+                deposit_group(A, W, cx, cy, dxl, dyl, 1u, fx, fy, fxy);
             }
         }
     }
     if (DEPOSIT && AGG) {
         if (warp_group_sum(gcnt ? gkey : -1, gcnt, gfx, gfy, gxy) && gcnt)
-            deposit_group(A, W, gcx, gcy, gcnt, gfx, gfy, gxy);
+            deposit_group(A, W, gkey & 0xFFFF, gkey >> 16, gdx, gdy, gcnt, gfx, gfy, gxy);
     } else if (DEPOSIT && gcnt) {
-        deposit_group(A, W, gcx, gcy, gcnt, gfx, gfy, gxy);
+        deposit_group(A, W, gkey & 0xFFFF, gkey >> 16, gdx, gdy, gcnt, gfx, gfy, gxy);
     }
 }
 
@@ -445,6 +468,8 @@ __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, 
             if (MOVE && live) store_quad(A, q, cc, xo, yo, xv, yv);
         }
     }
+    // a non-finite (or overflowing) velocity makes the sum of squares non-finite
+    if (MOVE) bad |= !(fabsf(ke) <= 3.0e38f);
     finish_block<DEPOSIT>(G, W, sAcc, ke, px, py, MOVE && bad);
 }
 
