@@ -310,15 +310,15 @@ def ens_fp64_check(P, cfgs, specs, nsteps, max_particles=8_000_000):
 # the ensemble's push chunk and sort cadence, and per (grid side, particles
 # per cell) a single handle's chunk, tile width, tile height and cadence.
 # The default line's ensemble record uses them and so needs no tuning runs.
-ENSEMBLE_TUNED = (16384, 20)
+ENSEMBLE_TUNED = (4096, 20)
 PLAIN_TUNED = {
-    (512, 256): (16384, 16, 4, 20), (512, 128): (8192, 16, 4, 10), (512, 64): (4096, 16, 4, 10),
+    (512, 256): (16384, 16, 4, 20), (512, 128): (8192, 16, 4, 10), (512, 64): (8192, 16, 8, 10),
     (512, 32): (4096, 16, 8, 10), (512, 16): (4096, 16, 16, 10), (256, 256): (8192, 16, 2, 20),
-    (256, 128): (8192, 16, 4, 20), (256, 64): (4096, 16, 4, 40), (256, 32): (4096, 16, 8, 20),
-    (256, 16): (4096, 16, 16, 20), (128, 256): (4096, 16, 1, 40), (128, 128): (4096, 16, 2, 40),
-    (128, 64): (4096, 16, 4, 40), (128, 32): (4096, 16, 8, 40), (128, 16): (4096, 16, 16, 40),
+    (256, 128): (8192, 16, 4, 20), (256, 64): (4096, 16, 4, 20), (256, 32): (4096, 16, 8, 10),
+    (256, 16): (4096, 16, 16, 20), (128, 256): (4096, 16, 1, 40), (128, 128): (4096, 16, 2, 20),
+    (128, 64): (4096, 16, 4, 80), (128, 32): (4096, 16, 8, 40), (128, 16): (4096, 16, 16, 40),
     (64, 256): (4096, 16, 1, 40), (64, 128): (4096, 16, 2, 40), (64, 64): (4096, 16, 4, 80),
-    (64, 32): (4096, 16, 8, 80), (64, 16): (4096, 16, 16, 80)}
+    (64, 32): (4096, 16, 8, 40), (64, 16): (4096, 16, 16, 80)}
 
 
 def whole_periods(steps, cadences):

@@ -186,8 +186,10 @@ pic_status pic_set_particles(pic_handle *h, int species, long long n, const doub
 pic_status pic_get_particles(pic_handle *h, int species, long long *n, double *x, double *y,
                              double *vx, double *vy, double *vz);
 
-/* Copy a species' raw device storage to host arrays in storage order (the
- * sorted order, not id order); any array may be NULL. */
+/* Copy a species' raw device storage to host arrays in storage order, not
+ * id order: after a sort the DSMC species is ordered by cell, every other
+ * species by tile and, within a tile, by cell row (tile-major cell index /
+ * tile_w); any array may be NULL. */
 pic_status pic_get_particles_raw(pic_handle *h, int species, long long *n, int32_t *cell,
                                  float *ox, float *oy, float *vx, float *vy, uint32_t *pid);
 
@@ -207,7 +209,8 @@ pic_status pic_particles_device(pic_handle *h, int species, pic_particles_view *
 pic_status pic_prime_leapfrog(pic_handle *h);
 
 /* ---- the step stages ---- */
-pic_status pic_sort(pic_handle *h);    /* counting sort of every species by cell tile */
+pic_status pic_sort(pic_handle *h);    /* counting sort of every species: by tile row,
+                                          the DSMC species by cell */
 pic_status pic_deposit(pic_handle *h); /* fixed-point rho from the current positions  */
 pic_status pic_poisson(pic_handle *h); /* rho -> E (cuFFT R2C, k-space kernel, C2R)   */
 /* Gather E, push every species one step; with deposit != 0 the new charge
