@@ -446,6 +446,18 @@ __device__ __forceinline__ void push_block(const PushArgs &A, const PushGeo &G, 
         for (long long qw = base + 4ll * (threadIdx.x & ~31u); qw < end; qw += stride) {
             const long long q = qw + lane4;
             const bool live = q < end;
+            // the thread's quad of the next iteration, fetched into L2 now so
+            // that its loads wait on L2 rather than DRAM (no registers held;
+            // measured at 2048^2: 0.958 against 1.000 ms per launch, and
+            // 0.970 ms two iterations ahead)
+            if (MOVE && q + stride < end) {
+                const long long qn = q + stride;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(A.cin + qn));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(A.oxin + qn));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(A.oyin + qn));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(A.vxin + qn));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(A.vyin + qn));
+            }
             // plain (coherent) loads: with an in-place pass the same addresses are stored below
             int cc[4] = {-1, -1, -1, -1};
             float xo[4] = {0.f, 0.f, 0.f, 0.f}, yo[4] = {0.f, 0.f, 0.f, 0.f};
