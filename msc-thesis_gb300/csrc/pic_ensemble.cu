@@ -73,22 +73,40 @@ __device__ __forceinline__ KeyGeo run_geo(const EnsRun &R, int rows)
     return key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off, rows);
 }
 
+// The sort kernels loop over the sort-block table with a grid of resident
+// blocks, each fetching its next table entry's particles into L2 while it
+// works on the current one.
 __global__ void __launch_bounds__(SORT_THREADS)
-ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
+ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs,
+                     int nblk)
 {
     __shared__ SortSmem S;
-    const SegBlock b = blk[blockIdx.x];
-    sort_hist_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
+    for (int i = blockIdx.x; i < nblk; i += gridDim.x) {
+        if (i + (int)gridDim.x < nblk) {
+            const SegBlock nb = blk[i + gridDim.x];
+            prefetch_chunk(A, nb.base, nb.base + nb.count, false);
+        }
+        const SegBlock b = blk[i];
+        sort_hist_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
+        __syncthreads();  // the next entry clears the counts
+    }
 }
 
 __global__ void __launch_bounds__(SORT_THREADS, 4)
 ens_sort_scatter_kernel(SortArgs A, const SegBlock *__restrict__ blk,
-                        const EnsRun *__restrict__ runs)
+                        const EnsRun *__restrict__ runs, int nblk)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem);
-    const SegBlock b = blk[blockIdx.x];
-    sort_scatter_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
+    for (int i = blockIdx.x; i < nblk; i += gridDim.x) {
+        if (i + (int)gridDim.x < nblk) {
+            const SegBlock nb = blk[i + gridDim.x];
+            prefetch_chunk(A, nb.base, nb.base + nb.count, true);
+        }
+        const SegBlock b = blk[i];
+        sort_scatter_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
+        __syncthreads();  // the next entry reuses the shared memory
+    }
 }
 
 // tile of the first particle of every push block, from the sorted buffer
@@ -517,12 +535,14 @@ pic_status ens_sort(pic_ensemble *E, const float *const *xin, float *const *xout
     cudaStream_t st = E->stream;
     const SortArgs A = ens_sort_args(E, xin, xout);
     PIC_CUDA(cudaMemsetAsync(E->count, 0, sizeof(uint32_t) * (size_t)E->nkeys, st));
-    ens_sort_hist_kernel<<<E->nsort, SORT_THREADS, 0, st>>>(A, E->sort_blk, E->d_runs);
+    ens_sort_hist_kernel<<<sort_grid(E->nsort, 6), SORT_THREADS, 0, st>>>(A, E->sort_blk, E->d_runs,
+                                                                        E->nsort);
     PIC_CUDA(cudaGetLastError());
     PIC_TRY(launch_key_scan(E->count, E->offset, E->cursor, E->nkeys, E->bsum, E->bsum_s, E->bsum2,
                             E->d_total, st));
     PIC_TRY(scatter_smem_attr((const void *)ens_sort_scatter_kernel));
-    ens_sort_scatter_kernel<<<E->nsort, SORT_THREADS, SCATTER_SMEM, st>>>(A, E->sort_blk, E->d_runs);
+    ens_sort_scatter_kernel<<<sort_grid(E->nsort, 4), SORT_THREADS, SCATTER_SMEM, st>>>(
+        A, E->sort_blk, E->d_runs, E->nsort);
     PIC_CUDA(cudaGetLastError());
     if (E->npush) {
         ens_anchor_kernel<<<(E->npush + 255) / 256, 256, 0, st>>>(E->cell[1], E->push_blk, E->d_runs,

@@ -42,7 +42,7 @@ pic_status cufft_fail(cufftResult r, const char *what)
     return (r == CUFFT_ALLOC_FAILED) ? PIC_ERR_OOM : PIC_ERR_CUFFT;
 }
 
-int grid_for(long long n, int block)
+int device_sms()
 {
     static int sms = 0;
     if (!sms) {
@@ -52,6 +52,12 @@ int grid_for(long long n, int block)
             sms <= 0)
             sms = 152;
     }
+    return sms;
+}
+
+int grid_for(long long n, int block)
+{
+    const int sms = device_sms();
     long long b = (n + block - 1) / block;
     const long long cap = (long long)sms * 8;
     if (b > cap) b = cap;

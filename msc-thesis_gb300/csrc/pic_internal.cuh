@@ -287,6 +287,8 @@ pic_status launch_to_global_target(const InitTarget &T, const long long *d_n, lo
 
 // grid-stride launch size for `n` items on the current device
 int grid_for(long long n, int block);
+int device_sms();  // multiprocessors of the current device (cached; 152 if unknown)
+unsigned sort_grid(long long chunks, int per_sm);  // sort blocks: at most the resident ones
 
 // pic_handle.cu stages used by other host files
 pic_status record_poisson(pic_handle *h, int adv = ADV_FIELD);

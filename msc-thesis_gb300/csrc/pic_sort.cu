@@ -38,25 +38,45 @@
 
 namespace pic {
 
-constexpr int HIST_SUB = 4;  // sort chunks per histogram block of a single run
+constexpr int HIST_SUB = 4;  // sort chunks per histogram iteration of a single run
+// resident blocks per SM that the sort grids are sized for: each block
+// loops over chunks and prefetches its next chunk into L2 while it counts or
+// moves the current one
+constexpr int HIST_BLOCKS_PER_SM = 6;
+constexpr int SCATTER_BLOCKS_PER_SM = 4;
 
 __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
 {
     __shared__ SortSmem S;
     const long long n = *A.d_n;
-    const long long base = (long long)blockIdx.x * (HIST_SUB * SORT_CHUNK);
-    if (base >= n) return;
-    sort_hist_block<HIST_SUB>(A, single_geo(A), S, base, n);
+    const long long span = (long long)HIST_SUB * SORT_CHUNK, stride = span * gridDim.x;
+    for (long long base = (long long)blockIdx.x * span; base < n; base += stride) {
+#pragma unroll
+        for (int u = 0; u < HIST_SUB; ++u)
+            prefetch_chunk(A, base + stride + (long long)u * SORT_CHUNK, n, false);
+        sort_hist_block<HIST_SUB>(A, single_geo(A), S, base, n);
+        __syncthreads();  // the next iteration clears the counts
+    }
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 4) sort_scatter_kernel(SortArgs A)
+__global__ void __launch_bounds__(SORT_THREADS, SCATTER_BLOCKS_PER_SM) sort_scatter_kernel(SortArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     ScatterSmem &S = *reinterpret_cast<ScatterSmem *>(smem);
     const long long n = *A.d_n;
-    const long long base = (long long)blockIdx.x * SORT_CHUNK;
-    if (base >= n) return;
-    sort_scatter_block(A, single_geo(A), S, base, n);
+    const long long stride = (long long)SORT_CHUNK * gridDim.x;
+    for (long long base = (long long)blockIdx.x * SORT_CHUNK; base < n; base += stride) {
+        prefetch_chunk(A, base + stride, n, true);
+        sort_scatter_block(A, single_geo(A), S, base, n);
+        __syncthreads();  // the next iteration reuses the shared memory
+    }
+}
+
+// blocks of a sort launch over `chunks` chunks: at most the resident blocks
+unsigned sort_grid(long long chunks, int per_sm)
+{
+    const long long cap = (long long)device_sms() * per_sm;
+    return (unsigned)std::max(1ll, std::min(chunks, cap));
 }
 
 // Exclusive scan, stage 1: each block scans 4096 entries (4 per thread).
@@ -298,7 +318,8 @@ static pic_status launch_hist(pic_handle *h, int s, const SortArgs &A)
     const SpeciesBuf &B = h->sp[s];
     PIC_CUDA(cudaMemsetAsync(A.count, 0, sizeof(uint32_t) * (size_t)A.nkeys, h->stream));
     const long long hc = (long long)HIST_SUB * SORT_CHUNK;
-    sort_hist_kernel<<<(unsigned)((B.cap + hc - 1) / hc), SORT_THREADS, 0, h->stream>>>(A);
+    sort_hist_kernel<<<sort_grid((B.cap + hc - 1) / hc, HIST_BLOCKS_PER_SM), SORT_THREADS, 0,
+                       h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }
@@ -322,7 +343,7 @@ pic_status launch_sort(pic_handle *h, int s, bool counts_kept)
     const bool dsmc = h->dsmc.on && s == h->dsmc.s && h->dsmc.count;
     const long long nkeys = A.nkeys;
     PIC_CUDA(cudaMemsetAsync(B.anchor, 0xFF, sizeof(int32_t) * (size_t)B.nchunks, h->stream));
-    const unsigned gp = (unsigned)((B.cap + SORT_CHUNK - 1) / SORT_CHUNK);
+    const unsigned gp = sort_grid((B.cap + SORT_CHUNK - 1) / SORT_CHUNK, SCATTER_BLOCKS_PER_SM);
     if (!(dsmc && counts_kept)) PIC_TRY(launch_hist(h, s, A));
     scan_blocks_kernel<<<h->scan_blocks, 1024, 0, h->stream>>>(A.count, h->offset, nkeys, h->bsum);
     PIC_CUDA(cudaGetLastError());

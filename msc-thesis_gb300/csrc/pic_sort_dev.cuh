@@ -201,6 +201,29 @@ __device__ __forceinline__ long long quad_start(long long base)
     return base + (long long)SORT_PER_THREAD * threadIdx.x;
 }
 
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// This thread's quad of the chunk at `base` fetched into L2 ahead of its
+// use by a later iteration of the same block: the cells, or every field
+// the scatter moves.  No registers are held.
+__device__ __forceinline__ void prefetch_chunk(const SortArgs &A, long long base, long long end,
+                                               bool fields)
+{
+    const long long q = quad_start(base);
+    if (q >= end) return;
+    prefetch_l2(A.cin + q);
+    if (!fields) return;
+    prefetch_l2(A.oxin + q);
+    prefetch_l2(A.oyin + q);
+    prefetch_l2(A.vxin + q);
+    prefetch_l2(A.vyin + q);
+    prefetch_l2(A.pidin + q);
+    if (A.vzin) prefetch_l2(A.vzin + q);
+}
+
 // The thread's quad of cells (one 128-bit load); slots at or past `end` get
 // INT_MIN (no particle).
 __device__ __forceinline__ void load_cells(const SortArgs &A, long long base, long long end,
