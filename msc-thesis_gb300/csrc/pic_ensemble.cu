@@ -76,7 +76,7 @@ __device__ __forceinline__ KeyGeo run_geo(const EnsRun &R, int rows)
 // The sort kernels loop over the sort-block table with a grid of resident
 // blocks, each fetching its next table entry's particles into L2 while it
 // works on the current one.
-__global__ void __launch_bounds__(SORT_THREADS)
+__global__ void __launch_bounds__(SORT_THREADS, 6)
 ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs,
                      int nblk)
 {

@@ -45,7 +45,7 @@ constexpr int HIST_SUB = 4;  // sort chunks per histogram iteration of a single 
 constexpr int HIST_BLOCKS_PER_SM = 6;
 constexpr int SCATTER_BLOCKS_PER_SM = 4;
 
-__global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
+__global__ void __launch_bounds__(SORT_THREADS, HIST_BLOCKS_PER_SM) sort_hist_kernel(SortArgs A)
 {
     __shared__ SortSmem S;
     const long long n = *A.d_n;
