@@ -73,24 +73,17 @@ __device__ __forceinline__ KeyGeo run_geo(const EnsRun &R, int rows)
     return key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off, rows);
 }
 
-// The sort kernels loop over the sort-block table with a grid of resident
-// blocks, each fetching its next table entry's particles into L2 while it
-// works on the current one.
-__global__ void __launch_bounds__(SORT_THREADS, 6)
-ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs,
-                     int nblk)
+__global__ void __launch_bounds__(SORT_THREADS)
+ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
 {
     __shared__ SortSmem S;
-    for (int i = blockIdx.x; i < nblk; i += gridDim.x) {
-        if (i + (int)gridDim.x < nblk) {
-            const SegBlock nb = blk[i + gridDim.x];
-            prefetch_chunk(A, nb.base, nb.base + nb.count, false);
-        }
-        const SegBlock b = blk[i];
-        sort_hist_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
-        __syncthreads();  // the next entry clears the counts
-    }
+    const SegBlock b = blk[blockIdx.x];
+    sort_hist_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
 }
+
+// The scatter loops over the sort-block table with a grid of resident
+// blocks, each fetching its next table entry's particles into L2 while it
+// moves the current one.
 
 __global__ void __launch_bounds__(SORT_THREADS, 4)
 ens_sort_scatter_kernel(SortArgs A, const SegBlock *__restrict__ blk,
@@ -535,8 +528,7 @@ pic_status ens_sort(pic_ensemble *E, const float *const *xin, float *const *xout
     cudaStream_t st = E->stream;
     const SortArgs A = ens_sort_args(E, xin, xout);
     PIC_CUDA(cudaMemsetAsync(E->count, 0, sizeof(uint32_t) * (size_t)E->nkeys, st));
-    ens_sort_hist_kernel<<<sort_grid(E->nsort, 6), SORT_THREADS, 0, st>>>(A, E->sort_blk, E->d_runs,
-                                                                        E->nsort);
+    ens_sort_hist_kernel<<<E->nsort, SORT_THREADS, 0, st>>>(A, E->sort_blk, E->d_runs);
     PIC_CUDA(cudaGetLastError());
     PIC_TRY(launch_key_scan(E->count, E->offset, E->cursor, E->nkeys, E->bsum, E->bsum_s, E->bsum2,
                             E->d_total, st));
