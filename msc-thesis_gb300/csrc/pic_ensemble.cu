@@ -73,12 +73,16 @@ __device__ __forceinline__ KeyGeo run_geo(const EnsRun &R, int rows)
     return key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off, rows);
 }
 
+// histogram blocks count four sort chunks of one run with all loads issued
+// first (2.45 ms per sort over the 64 runs with one chunk per block)
+constexpr int ENS_HIST_SUB = 4;
+
 __global__ void __launch_bounds__(SORT_THREADS)
 ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
 {
     __shared__ SortSmem S;
     const SegBlock b = blk[blockIdx.x];
-    sort_hist_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
+    sort_hist_block<ENS_HIST_SUB>(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
 }
 
 // The scatter loops over the sort-block table with a grid of resident
@@ -218,7 +222,7 @@ void ens_free(pic_ensemble *E)
                     E->vx[0], E->vx[1], E->vy[0], E->vy[1], E->pid[0], E->pid[1], E->rho_fix,
                     E->rho, E->e, E->rhohat, E->ehat, E->count, E->offset, E->cursor, E->bsum,
                     E->bsum_s, E->bsum2, E->d_total, E->push_blk, E->sort_blk, E->node_blk,
-                    E->mode_blk, E->anchor, E->dev, E->hist, E->stage};
+                    E->mode_blk, E->hist_blk, E->anchor, E->dev, E->hist, E->stage};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &G : E->groups) {
@@ -263,7 +267,7 @@ pic_status ens_layout(pic_ensemble *E)
     E->runs.resize(nr);
     long long poff = 0, goff = 0, khoff = 0;
     long long koff = 0;
-    std::vector<SegBlock> sb, nb, mb;
+    std::vector<SegBlock> sb, nb, mb, hb;
     for (int s = 0; s < nr; ++s) {
         const pic_config &c = E->cfg[order[s]];
         const pic_species_desc &D = c.species[0];
@@ -315,6 +319,7 @@ pic_status ens_layout(pic_ensemble *E)
         khoff += 2 * R.nk;
         koff += ncell + 1;
         add_blocks(sb, s, R.poff, R.cap4, SORT_CHUNK);
+        add_blocks(hb, s, R.poff, R.cap4, ENS_HIST_SUB * SORT_CHUNK);
         add_blocks(nb, s, 0, R.ncp, ENS_NODES_PER_BLOCK);
         add_blocks(mb, s, 0, R.nk, ENS_NODES_PER_BLOCK);
     }
@@ -323,6 +328,8 @@ pic_status ens_layout(pic_ensemble *E)
     E->nmodes = khoff;
     E->nkeys = koff;
     PIC_TRY(upload(&E->sort_blk, sb));
+    PIC_TRY(upload(&E->hist_blk, hb));
+    E->nhist = (int)hb.size();
     PIC_TRY(upload(&E->node_blk, nb));
     PIC_TRY(upload(&E->mode_blk, mb));
     E->nsort = (int)sb.size();
@@ -528,7 +535,7 @@ pic_status ens_sort(pic_ensemble *E, const float *const *xin, float *const *xout
     cudaStream_t st = E->stream;
     const SortArgs A = ens_sort_args(E, xin, xout);
     PIC_CUDA(cudaMemsetAsync(E->count, 0, sizeof(uint32_t) * (size_t)E->nkeys, st));
-    ens_sort_hist_kernel<<<E->nsort, SORT_THREADS, 0, st>>>(A, E->sort_blk, E->d_runs);
+    ens_sort_hist_kernel<<<E->nhist, SORT_THREADS, 0, st>>>(A, E->hist_blk, E->d_runs);
     PIC_CUDA(cudaGetLastError());
     PIC_TRY(launch_key_scan(E->count, E->offset, E->cursor, E->nkeys, E->bsum, E->bsum_s, E->bsum2,
                             E->d_total, st));

@@ -63,7 +63,8 @@ struct pic_ensemble {
     long long *d_total = nullptr;
     // work tables
     pic::SegBlock *push_blk = nullptr, *sort_blk = nullptr, *node_blk = nullptr, *mode_blk = nullptr;
-    int npush = 0, nsort = 0, nnode_blk = 0, nmode_blk = 0;
+    pic::SegBlock *hist_blk = nullptr;  // histogram blocks: four sort chunks of one run
+    int npush = 0, nsort = 0, nnode_blk = 0, nmode_blk = 0, nhist = 0;
     int32_t *anchor = nullptr;
     size_t push_smem = 0;
     // diagnostics
