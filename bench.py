@@ -676,7 +676,8 @@ def main():
     ap.add_argument("--tile", type=int, nargs=2, default=(0, 0))
     ap.add_argument("--sort-every", type=int, default=SORT_EVERY)
     ap.add_argument("--halo", type=int, default=0, help="push window halo in cells (0: the library's)")
-    ap.add_argument("--push-variant", type=int, default=0, help="0 auto, 1 direct, 2 bulk copy")
+    ap.add_argument("--push-variant", type=int, default=0,
+                    help="0 auto, 1 direct, 3 warp-summed deposit groups")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (untimed setup)")
     ap.add_argument("--adjoint-steps", type=int, default=500,
                     help="ensemble workload: steps of the timed forward+adjoint (0: skip)")
