@@ -241,7 +241,7 @@ pic_status launch_kspace(pic_handle *h, bool phi_only, float2 *phihat);
 enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
 // pic_sort.cu
-pic_status launch_sort(pic_handle *h, int s, bool counts_kept = false, int from = 0);
+pic_status launch_sort(pic_handle *h, int s, bool counts_kept = false);
 pic_status launch_recount(pic_handle *h, int s);
 void sort_sizes_for(double density, int *wk, int *hb);
 pic_status scatter_smem_attr(const void *kernel);
