@@ -98,7 +98,7 @@ ens_sort_scatter_kernel(SortArgs A, const SegBlock *__restrict__ blk,
     for (int i = blockIdx.x; i < nblk; i += gridDim.x) {
         if (i + (int)gridDim.x < nblk) {
             const SegBlock nb = blk[i + gridDim.x];
-            prefetch_chunk(A, nb.base, nb.base + nb.count, true);
+            prefetch_chunk(A, nb.base, nb.base + nb.count);
         }
         const SegBlock b = blk[i];
         sort_scatter_block(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);

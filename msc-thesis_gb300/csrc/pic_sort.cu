@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(SORT_THREADS, SCATTER_BLOCKS_PER_SM) sort_scat
     const long long n = *A.d_n;
     const long long stride = (long long)SORT_CHUNK * gridDim.x;
     for (long long base = (long long)blockIdx.x * SORT_CHUNK; base < n; base += stride) {
-        prefetch_chunk(A, base + stride, n, true);
+        prefetch_chunk(A, base + stride, n);
         sort_scatter_block(A, single_geo(A), S, base, n);
         __syncthreads();  // the next iteration reuses the shared memory
     }

@@ -206,16 +206,14 @@ __device__ __forceinline__ void prefetch_l2(const void *p)
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
-// This thread's quad of the chunk at `base` fetched into L2 ahead of its
-// use by a later iteration of the same block: the cells, or every field
-// the scatter moves.  No registers are held.
-__device__ __forceinline__ void prefetch_chunk(const SortArgs &A, long long base, long long end,
-                                               bool fields)
+// This thread's quad of every field the scatter moves, for the chunk at
+// `base`, fetched into L2 ahead of its use by a later iteration of the same
+// block.  No registers are held.
+__device__ __forceinline__ void prefetch_chunk(const SortArgs &A, long long base, long long end)
 {
     const long long q = quad_start(base);
     if (q >= end) return;
     prefetch_l2(A.cin + q);
-    if (!fields) return;
     prefetch_l2(A.oxin + q);
     prefetch_l2(A.oyin + q);
     prefetch_l2(A.vxin + q);
