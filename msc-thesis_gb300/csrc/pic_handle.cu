@@ -116,6 +116,7 @@ static void free_handle_buffers(pic_handle *h)
     cudaFree(h->rhohat);
     cudaFree(h->ehat);
     cudaFree(h->e);
+    cudaFree(h->tw);
     cudaFree(h->count);
     cudaFree(h->offset);
     cudaFree(h->cursor);
@@ -257,10 +258,14 @@ static void update_mean(pic_handle *h)
 // ADV_PUSH | ADV_FIELD when the particle pass left its fold to this launch)
 pic_status record_poisson(pic_handle *h, int adv)
 {
-    PIC_TRY(launch_convert(h));
-    PIC_CUFFT(cufftExecR2C(h->plan_r2c, h->rho, (cufftComplex *)h->rhohat));
-    PIC_TRY(launch_kspace(h, false, nullptr));
-    PIC_CUFFT(cufftExecC2R(h->plan_c2r2, (cufftComplex *)h->ehat, h->e));
+    if (h->spectral) {
+        PIC_TRY(launch_spectral(h));
+    } else {
+        PIC_TRY(launch_convert(h));
+        PIC_CUFFT(cufftExecR2C(h->plan_r2c, h->rho, (cufftComplex *)h->rhohat));
+        PIC_TRY(launch_kspace(h, false, nullptr));
+        PIC_CUFFT(cufftExecC2R(h->plan_c2r2, (cufftComplex *)h->ehat, h->e));
+    }
     PIC_TRY(launch_advance(h, adv));
     return PIC_OK;
 }
@@ -663,6 +668,11 @@ pic_status pic_create(const pic_config *cfg, pic_handle **out)
     H_CUFFT(cufftSetStream(h->plan_r2c, h->stream));
     H_CUFFT(cufftSetStream(h->plan_c2r2, h->stream));
     H_CUFFT(cufftSetStream(h->plan_c2r1, h->stream));
+    // the step's solve: the spectral kernels on power-of-two grids, unless
+    // PIC_FIELD_SOLVER=cufft asks for the library transforms
+    const char *solver = getenv("PIC_FIELD_SOLVER");
+    h->spectral = spectral_size_ok(g.nx, g.ny) && !(solver && strcmp(solver, "cufft") == 0);
+    if (h->spectral) H_TRY(spectral_tables(h));
     H_TRY(reset_device_state(h));
 #undef H_TRY
 #undef H_CUDA
@@ -1054,8 +1064,11 @@ pic_status pic_get_grid(pic_handle *h, int which, double *out)
     } else if (which == PIC_GRID_EY) {
         src = h->e + ncell;
     } else {
-        // phi^ into the first half of ehat, C2R into the second half
+        // phi^ into the first half of ehat, C2R into the second half (the
+        // spectral solve leaves no full spectrum: transform rho first)
         const size_t nk = (size_t)h->g.ny * h->g.nh;
+        if (h->spectral)
+            PIC_CUFFT(cufftExecR2C(h->plan_r2c, h->rho, (cufftComplex *)h->rhohat));
         PIC_TRY(launch_kspace(h, true, h->ehat));
         PIC_CUFFT(cufftExecC2R(h->plan_c2r1, (cufftComplex *)h->ehat, (cufftReal *)(h->ehat + nk)));
         src = (const float *)(h->ehat + nk);

@@ -191,6 +191,10 @@ struct pic_handle {
     float2 *ehat = nullptr;                  // 2*ny*nh
     float *e = nullptr;                      // 2*nx*ny: Ex plane then Ey plane
     cufftHandle plan_r2c = 0, plan_c2r2 = 0, plan_c2r1 = 0;
+    // power-of-two grids: the step's solve runs in pic_spectral.cu's kernels
+    // (rhohat and ehat then hold their column-major intermediates)
+    bool spectral = false;
+    float2 *tw = nullptr;  // twiddles: nx entries, then ny
     // sort
     uint32_t *count = nullptr, *offset = nullptr, *cursor = nullptr, *bsum = nullptr;
     int scan_blocks = 0;
@@ -233,6 +237,10 @@ pic_status launch_convert(pic_handle *h);
 pic_status launch_kspace(pic_handle *h, bool phi_only, float2 *phihat);
 enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
+// pic_spectral.cu
+bool spectral_size_ok(int nx, int ny);
+pic_status spectral_tables(pic_handle *h);
+pic_status launch_spectral(pic_handle *h);  // convert + solve, rho_fix cleared
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s, bool counts_kept = false);
 pic_status launch_recount(pic_handle *h, int s);
