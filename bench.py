@@ -2,9 +2,10 @@
 """Throughput of the 2-D electrostatic PIC step on GB300 (particle-steps/s).
 
 Workload (one "step" = one PIC time step: gather + push + fixed-point deposit
-of every particle, int64->float density, cuFFT R2C, k-space kernel, 2x C2R,
-a counting sort every `sort_every` steps): the large collisionless run,
-2048 x 2048 periodic cells, 32 electrons per cell (134,217,728 particles),
+of every particle, the spectral Poisson solve (density conversion, FFTs and
+k-space operator in three kernels), a counting sort every `sort_every`
+steps): the large collisionless run, 2048 x 2048 periodic cells, 32
+electrons per cell (134,217,728 particles),
 Maxwellian vth = 0.05 with a density perturbation of amplitude 0.01 in mode
 (1,1), dt = 0.05, plasma units (eps0 = 1, omega_pe = 1), L = 2048 * 0.05.
 Data are synthetic (seeded Philox init).  The particle arrays (2.7 GB per
@@ -69,6 +70,47 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def gpu_local_cpus(index):
+    """Host cores attached to GPU `index` (the local_cpulist of its PCI
+    device), within the cores this process may use; None if unknown."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(index), "--query-gpu=pci.bus_id",
+                              "--format=csv,noheader"], capture_output=True, text=True,
+                             timeout=30).stdout.strip()
+        dom, rest = bus.split(":", 1)  # 00000009:01:00.0 -> 0009:01:00.0
+        path = f"/sys/bus/pci/devices/{dom[-4:].lower()}:{rest.lower()}/local_cpulist"
+        cpus = set()
+        with open(path) as f:
+            for part in f.read().strip().split(","):
+                a, _, b = part.partition("-")
+                cpus.update(range(int(a), int(b or a) + 1))
+        cpus &= os.sched_getaffinity(0)
+        return cpus or None
+    except Exception:
+        return None
+
+
+def link_rates(torch, hin, hout):
+    """GB/s of plain pinned host <-> device copies of the e2e buffers, on the
+    current stream (the link the e2e call's import and export cross)."""
+    dev = torch.empty_like(hin[0], device="cuda")
+    for x in hin[:1]:
+        dev.copy_(x, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for x in hin:
+        dev.copy_(x, non_blocking=True)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for y in hout:
+        y.copy_(dev, non_blocking=True)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    nbytes = sum(x.numel() * x.element_size() for x in hin)
+    del dev
+    return {"h2d": nbytes / (t1 - t0) / 1e9, "d2h": nbytes / (t2 - t1) / 1e9}
 
 
 class Clocks:
@@ -147,12 +189,14 @@ def schedule(k, since_sort, S):
     return sorts, since_sort
 
 
-def launches_for(k, since_sort, S, nspecies=1, per_sort=6):
-    """Our kernels launched by k steps: per step nspecies pushes + 2 advance +
-    convert + kspace; per sort and species histogram, 3 scan kernels, the
-    scatter and the anchor kernel.  Returns (count, sorts, since_sort)."""
+def launches_for(k, since_sort, S, per_step, nspecies=1, per_sort=6):
+    """Our kernels launched by k steps: per_step per step (single handle on a
+    power-of-two grid: push, the three spectral-solve kernels, one
+    diagnostics fold; ensemble: push, convert, k-space, two folds); per sort
+    and species histogram, 3 scan kernels, the scatter and the anchor kernel.
+    Returns (count, sorts, since_sort)."""
     sorts, after = schedule(k, since_sort, S)
-    return sorts * per_sort * nspecies + k * (nspecies + 4), sorts, after
+    return sorts * per_sort * nspecies + k * per_step, sorts, after
 
 
 def cpu_sample():
@@ -486,7 +530,7 @@ def bench_ensemble(args):
     ens_value = R.whole_job_rate(total_all * steps, ms / 1000.0)
     nb1 = -(-sum(int(g) * int(g) + 1 for g in grids) // 4096)
     per_sort = 6 if nb1 <= 4096 else 8  # two-level scan above 4096 block sums
-    ens_launches, ens_sorts, _ = launches_for(steps, S, S, per_sort=per_sort)
+    ens_launches, ens_sorts, _ = launches_for(steps, S, S, 5, per_sort=per_sort)
     plain_ms = m["plain_ms"]
     plain_value = R.whole_job_rate(total_all * steps, plain_ms / 1000.0) if plain_ms else None
     adj = ensemble_adjoint_rate(P, R, cfgs, specs, total_all, args.adjoint_steps, args.every, pg) \
@@ -661,7 +705,7 @@ def bench_small(args):
 
 
 def main():
-    global NX, NY, N, L, SORT_EVERY
+    global NX, NY, N, L, SORT_EVERY, PPC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=80)
@@ -672,6 +716,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true",
                     help="default workload: skip the batched-ensemble record")
     ap.add_argument("--nx", type=int, default=NX, help="cells per side (profiling on smaller cases)")
+    ap.add_argument("--ppc", type=int, default=PPC,
+                    help="particles per cell (profiling on smaller cases)")
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--tile", type=int, nargs=2, default=(0, 0))
     ap.add_argument("--sort-every", type=int, default=SORT_EVERY)
@@ -694,6 +740,7 @@ def main():
                          "dsmc: mcc plus DSMC neutrals")
     args = ap.parse_args()
     NX = NY = args.nx
+    PPC = args.ppc
     N = NX * NY * PPC
     L = NX * DX
     SORT_EVERY = args.sort_every
@@ -800,23 +847,36 @@ def main():
     # copy out (pic_run_host)
     e2e = None
     if not args.no_e2e:
-        a = h.get_particles(0)
-        pin = lambda arr: torch.from_numpy(arr).pin_memory()
-        hin = [pin(a[k]) for k in ("x", "y", "vx", "vy")]
-        hout = [torch.empty(N, dtype=torch.float64).pin_memory() for _ in range(4)]
-        del a
-        # untimed warm-up call (the link's first touch of freshly pinned pages)
-        h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.warmup, 1,
-             *[x.data_ptr() for x in hout])
-        barrier()
-        t0 = time.perf_counter()
-        h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.steps, 1,
-             *[x.data_ptr() for x in hout])
-        el = R.max_over_ranks(time.perf_counter() - t0, pg, device="cuda")
-        e2e = {"value": R.whole_job_rate(world * N * args.steps, el), "unit": "particle-steps/s",
-               "h2d_bytes_per_step": 32 * N / args.steps, "d2h_bytes_per_step": 32 * N / args.steps,
-               "seconds": el, "steps": args.steps}
-        del hin, hout
+        # the host buffers are page-locked from a core attached to the GPU
+        # (first touch puts them in that core's memory, next to the link)
+        affinity = os.sched_getaffinity(0)
+        near = gpu_local_cpus(local)
+        if near:
+            os.sched_setaffinity(0, near)
+        try:
+            a = h.get_particles(0)
+            pin = lambda arr: torch.from_numpy(arr).pin_memory()
+            hin = [pin(a[k]) for k in ("x", "y", "vx", "vy")]
+            hout = [torch.empty(N, dtype=torch.float64).pin_memory() for _ in range(4)]
+            del a
+            # untimed warm-up call (the link's first touch of freshly pinned pages)
+            h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.warmup, 1,
+                 *[x.data_ptr() for x in hout])
+            barrier()
+            t0 = time.perf_counter()
+            h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.steps, 1,
+                 *[x.data_ptr() for x in hout])
+            el = R.max_over_ranks(time.perf_counter() - t0, pg, device="cuda")
+            e2e = {"value": R.whole_job_rate(world * N * args.steps, el),
+                   "unit": "particle-steps/s",
+                   "h2d_bytes_per_step": 32 * N / args.steps,
+                   "d2h_bytes_per_step": 32 * N / args.steps,
+                   "seconds": el, "steps": args.steps,
+                   "host_cores_bound": len(near) if near else None,
+                   "link_gbs": link_rates(torch, hin, hout)}
+            del hin, hout
+        finally:
+            os.sched_setaffinity(0, affinity)
 
     cpu = None
     fp64 = None
@@ -836,8 +896,8 @@ def main():
         if args.nx == NX:
             fp64 = fp64_check(P, cfg, spec, -A / N, A / N, 10)
 
-    _, _, since_after_warmup = launches_for(args.warmup + align, 0, SORT_EVERY)
-    launches, sorts_timed, _ = launches_for(args.steps, since_after_warmup, SORT_EVERY)
+    _, _, since_after_warmup = launches_for(args.warmup + align, 0, SORT_EVERY, 5)
+    launches, sorts_timed, _ = launches_for(args.steps, since_after_warmup, SORT_EVERY, 5)
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,

@@ -136,6 +136,9 @@ typedef struct pic_config {
 typedef struct pic_handle pic_handle;
 
 pic_status pic_config_default(pic_config *cfg);
+/* Power-of-two grids of 16..4096 cells a side solve the field with the
+ * library's spectral kernels, other sizes with cuFFT; the environment
+ * variable PIC_FIELD_SOLVER=cufft, read here, selects cuFFT for any size. */
 pic_status pic_create(const pic_config *cfg, pic_handle **out);
 pic_status pic_destroy(pic_handle *h);
 /* The CUDA stream all of the handle's work runs on (cudaStream_t). */
@@ -212,7 +215,7 @@ pic_status pic_prime_leapfrog(pic_handle *h);
 pic_status pic_sort(pic_handle *h);    /* counting sort of every species: by tile row,
                                           the DSMC species by cell */
 pic_status pic_deposit(pic_handle *h); /* fixed-point rho from the current positions  */
-pic_status pic_poisson(pic_handle *h); /* rho -> E (cuFFT R2C, k-space kernel, C2R)   */
+pic_status pic_poisson(pic_handle *h); /* rho -> E (spectral solve, see pic_create)    */
 /* Gather E, push every species one step; with deposit != 0 the new charge
  * density is deposited in the same pass (then pic_poisson gives E). */
 pic_status pic_gather_push(pic_handle *h, int deposit);

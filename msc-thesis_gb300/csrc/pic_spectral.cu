@@ -167,27 +167,28 @@ __global__ void __launch_bounds__(256, 2) spec_cols_kernel(SpecArgs A)
         b1[fft::pad(my)] = K.ey;
         fe += on ? K.fe : 0.f;
     }
-    {
-        float2 *buf[1] = {b0};
+    // the two inverse transforms share one copy of the code: s = 0 turns
+    // phi^ (registers, first buffer) into Ex~ = -i kx phi~ (Nyquist kx
+    // zeroed), s = 1 turns Ey^ (second buffer) into Ey~
+    const float kxe = (2 * mx == A.nx) ? 0.f : A.kx1 * (float)mx;
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+        float2 *const bs = s ? b1 : b0;
+        if (s) {
+            __syncthreads();  // Ey^ in the second buffer is complete
+#pragma unroll
+            for (int k = 0; k < fft::E; ++k) v[0][k] = b1[fft::pad(t + k * TP)];
+        }
+        float2 *buf[1] = {bs};
         fft::transform<LGY, true, 1>(v, buf, t, A.twy);
-    }
-    if (on) {
-        // Ex~ = -i kx (inverse of phi^), Nyquist kx zeroed
-        const float kxe = (2 * mx == A.nx) ? 0.f : A.kx1 * (float)mx;
+        if (on) {
+            float2 *const out = (s ? A.Ty : A.Tx) + col;
 #pragma unroll
-        for (int k = 0; k < fft::E; ++k)
-            A.Tx[col + fft::result_index<LGY>(k, t)] = make_float2(kxe * v[0][k].y, -kxe * v[0][k].x);
-    }
-    __syncthreads();  // Ey^ in the second buffer is complete
-#pragma unroll
-    for (int k = 0; k < fft::E; ++k) v[0][k] = b1[fft::pad(t + k * TP)];
-    {
-        float2 *buf[1] = {b1};
-        fft::transform<LGY, true, 1>(v, buf, t, A.twy);
-    }
-    if (on) {
-#pragma unroll
-        for (int k = 0; k < fft::E; ++k) A.Ty[col + fft::result_index<LGY>(k, t)] = v[0][k];
+            for (int k = 0; k < fft::E; ++k) {
+                const float2 u = v[0][k];
+                out[fft::result_index<LGY>(k, t)] = s ? u : make_float2(kxe * u.y, -kxe * u.x);
+            }
+        }
     }
     const double sum = block_sum((double)fe, s_fe);
     if (threadIdx.x == 0) atomicAdd(&A.dev->fe[acc_slot()], sum);
