@@ -72,26 +72,6 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def gpu_local_cpus(index):
-    """Host cores attached to GPU `index` (the local_cpulist of its PCI
-    device), within the cores this process may use; None if unknown."""
-    try:
-        bus = subprocess.run(["nvidia-smi", "-i", str(index), "--query-gpu=pci.bus_id",
-                              "--format=csv,noheader"], capture_output=True, text=True,
-                             timeout=30).stdout.strip()
-        dom, rest = bus.split(":", 1)  # 00000009:01:00.0 -> 0009:01:00.0
-        path = f"/sys/bus/pci/devices/{dom[-4:].lower()}:{rest.lower()}/local_cpulist"
-        cpus = set()
-        with open(path) as f:
-            for part in f.read().strip().split(","):
-                a, _, b = part.partition("-")
-                cpus.update(range(int(a), int(b or a) + 1))
-        cpus &= os.sched_getaffinity(0)
-        return cpus or None
-    except Exception:
-        return None
-
-
 def link_rates(torch, hin, hout):
     """GB/s of plain pinned host <-> device copies of the e2e buffers, on the
     current stream (the link the e2e call's import and export cross)."""
@@ -847,36 +827,32 @@ def main():
     # copy out (pic_run_host)
     e2e = None
     if not args.no_e2e:
-        # the host buffers are page-locked from a core attached to the GPU
-        # (first touch puts them in that core's memory, next to the link)
-        affinity = os.sched_getaffinity(0)
-        near = gpu_local_cpus(local)
-        if near:
-            os.sched_setaffinity(0, near)
-        try:
-            a = h.get_particles(0)
-            pin = lambda arr: torch.from_numpy(arr).pin_memory()
-            hin = [pin(a[k]) for k in ("x", "y", "vx", "vy")]
-            hout = [torch.empty(N, dtype=torch.float64).pin_memory() for _ in range(4)]
-            del a
-            # untimed warm-up call (the link's first touch of freshly pinned pages)
-            h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.warmup, 1,
-                 *[x.data_ptr() for x in hout])
-            barrier()
-            t0 = time.perf_counter()
-            h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.steps, 1,
-                 *[x.data_ptr() for x in hout])
-            el = R.max_over_ranks(time.perf_counter() - t0, pg, device="cuda")
-            e2e = {"value": R.whole_job_rate(world * N * args.steps, el),
-                   "unit": "particle-steps/s",
-                   "h2d_bytes_per_step": 32 * N / args.steps,
-                   "d2h_bytes_per_step": 32 * N / args.steps,
-                   "seconds": el, "steps": args.steps,
-                   "host_cores_bound": len(near) if near else None,
-                   "link_gbs": link_rates(torch, hin, hout)}
-            del hin, hout
-        finally:
-            os.sched_setaffinity(0, affinity)
+        # page-locked host buffers, allocated as such and checked (a buffer the
+        # driver did not see as page-locked would take the library's staged
+        # path for pageable arrays); plain copies of them time the link
+        a = h.get_particles(0)
+        hin = [torch.empty(N, dtype=torch.float64, pin_memory=True) for _ in range(4)]
+        for x, k in zip(hin, ("x", "y", "vx", "vy")):
+            x.numpy()[:] = a[k]
+        hout = [torch.empty(N, dtype=torch.float64, pin_memory=True) for _ in range(4)]
+        del a
+        pinned = all(x.is_pinned() for x in hin + hout)
+        link_before = link_rates(torch, hin, hout)
+        # untimed warm-up call (the link's first touch of freshly pinned pages)
+        h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.warmup, 1,
+             *[x.data_ptr() for x in hout])
+        barrier()
+        t0 = time.perf_counter()
+        h._c("pic_run_host", N, *[x.data_ptr() for x in hin], args.steps, 1,
+             *[x.data_ptr() for x in hout])
+        el = R.max_over_ranks(time.perf_counter() - t0, pg, device="cuda")
+        e2e = {"value": R.whole_job_rate(world * N * args.steps, el),
+               "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 32 * N / args.steps,
+               "d2h_bytes_per_step": 32 * N / args.steps,
+               "seconds": el, "steps": args.steps, "page_locked": pinned,
+               "link_gbs": {"before": link_before, "after": link_rates(torch, hin, hout)}}
+        del hin, hout
 
     cpu = None
     fp64 = None

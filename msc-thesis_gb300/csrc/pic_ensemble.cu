@@ -73,16 +73,13 @@ __device__ __forceinline__ KeyGeo run_geo(const EnsRun &R, int rows)
     return key_geo(R.nx, R.ny, R.tw, R.th, R.ntx, R.key_off, rows);
 }
 
-// histogram blocks count four sort chunks of one run with all loads issued
-// first (2.45 ms per sort over the 64 runs with one chunk per block)
-constexpr int ENS_HIST_SUB = 4;
-
+// histogram blocks count HIST_BLOCK consecutive particles of one run
 __global__ void __launch_bounds__(SORT_THREADS)
 ens_sort_hist_kernel(SortArgs A, const SegBlock *__restrict__ blk, const EnsRun *__restrict__ runs)
 {
-    __shared__ SortSmem S;
+    __shared__ uint32_t cnt[SORT_KEYS];
     const SegBlock b = blk[blockIdx.x];
-    sort_hist_block<ENS_HIST_SUB>(A, run_geo(runs[b.run], A.rows), S, b.base, b.base + b.count);
+    sort_hist_segments(A, run_geo(runs[b.run], A.rows), cnt, b.base, b.base + b.count);
 }
 
 // The scatter loops over the sort-block table with a grid of resident
@@ -319,7 +316,7 @@ pic_status ens_layout(pic_ensemble *E)
         khoff += 2 * R.nk;
         koff += ncell + 1;
         add_blocks(sb, s, R.poff, R.cap4, SORT_CHUNK);
-        add_blocks(hb, s, R.poff, R.cap4, ENS_HIST_SUB * SORT_CHUNK);
+        add_blocks(hb, s, R.poff, R.cap4, HIST_BLOCK);
         add_blocks(nb, s, 0, R.ncp, ENS_NODES_PER_BLOCK);
         add_blocks(mb, s, 0, R.nk, ENS_NODES_PER_BLOCK);
     }

@@ -38,20 +38,19 @@
 
 namespace pic {
 
-constexpr int HIST_SUB = 4;  // sort chunks per histogram block of a single run
 // resident scatter blocks per SM that its grid is sized for: each block
 // loops over chunks and prefetches its next chunk into L2 while it moves the
-// current one (the histogram measured slower that way: 370 against 317 us
-// at 2048^2, so it keeps one block per four chunks)
+// current one (the histogram, one block per HIST_BLOCK particles, measured
+// slower that way)
 constexpr int SCATTER_BLOCKS_PER_SM = 4;
 
 __global__ void __launch_bounds__(SORT_THREADS) sort_hist_kernel(SortArgs A)
 {
-    __shared__ SortSmem S;
+    __shared__ uint32_t cnt[SORT_KEYS];
     const long long n = *A.d_n;
-    const long long base = (long long)blockIdx.x * (HIST_SUB * SORT_CHUNK);
+    const long long base = (long long)blockIdx.x * HIST_BLOCK;
     if (base >= n) return;
-    sort_hist_block<HIST_SUB>(A, single_geo(A), S, base, n);
+    sort_hist_segments(A, single_geo(A), cnt, base, n);
 }
 
 __global__ void __launch_bounds__(SORT_THREADS, SCATTER_BLOCKS_PER_SM) sort_scatter_kernel(SortArgs A)
@@ -312,8 +311,8 @@ static pic_status launch_hist(pic_handle *h, int s, const SortArgs &A)
 {
     const SpeciesBuf &B = h->sp[s];
     PIC_CUDA(cudaMemsetAsync(A.count, 0, sizeof(uint32_t) * (size_t)A.nkeys, h->stream));
-    const long long hc = (long long)HIST_SUB * SORT_CHUNK;
-    sort_hist_kernel<<<(unsigned)((B.cap + hc - 1) / hc), SORT_THREADS, 0, h->stream>>>(A);
+    sort_hist_kernel<<<(unsigned)((B.cap + HIST_BLOCK - 1) / HIST_BLOCK), SORT_THREADS, 0,
+                       h->stream>>>(A);
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
 }

@@ -344,32 +344,60 @@ __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, S
     }
 }
 
-// Histogram of the keys of particles [base, end) (one sort block of SUB
-// consecutive SORT_CHUNK-particle sub-chunks: every quad's cells are loaded
-// before the first is counted, so that one block keeps SUB loads per
-// thread in flight and pays its barriers and window once).
-template <int SUB = 1>
-__device__ __forceinline__ void sort_hist_block(const SortArgs &A, const KeyGeo &G, SortSmem &S,
-                                                long long base, long long end)
+// Histogram of the keys of particles [base, end) (one block of HIST_BLOCK
+// consecutive particles): each thread counts the HIST_SEG consecutive
+// particles from base + HIST_SEG t, one atomic per run of equal keys, into a
+// shared window of wk keys around the block's middle key, or straight into
+// the global histogram outside it.  Particles sorted by key a few steps ago
+// make long runs: about one atomic per thread.  cnt: SORT_KEYS entries.
+constexpr int HIST_SEG = 16;
+constexpr int HIST_BLOCK = HIST_SEG * SORT_THREADS;
+
+__device__ __forceinline__ void sort_hist_segments(const SortArgs &A, const KeyGeo &G, uint32_t *cnt,
+                                                   long long base, long long end)
 {
-    const SortSizes Z = sort_sizes(A);
-    int keys[SUB][SORT_PER_THREAD];
+    const int wk = sort_sizes(A).wk;
+    const long long s0 = base + (long long)HIST_SEG * threadIdx.x;
+    int c[HIST_SEG];
 #pragma unroll
-    for (int u = 0; u < SUB; ++u) load_cells(A, base + (long long)u * SORT_CHUNK, end, keys[u]);
-    const int k0 = window_start(A, G, base, min(end, base + (long long)SUB * SORT_CHUNK), Z.wk);
-    init_smem(S, Z);
+    for (int u = 0; u < HIST_SEG / 4; ++u) {
+        const long long q = s0 + 4 * u;
+        int4 v = make_int4(INT_MIN, INT_MIN, INT_MIN, INT_MIN);
+        if (q < end) v = __ldg(reinterpret_cast<const int4 *>(A.cin + q));
+        c[4 * u] = v.x;
+        c[4 * u + 1] = q + 1 < end ? v.y : INT_MIN;
+        c[4 * u + 2] = q + 2 < end ? v.z : INT_MIN;
+        c[4 * u + 3] = q + 3 < end ? v.w : INT_MIN;
+    }
+    const int k0 = window_start(A, G, base, min(end, base + (long long)HIST_BLOCK), wk);
+    for (int r = threadIdx.x; r < wk; r += SORT_THREADS) cnt[r] = 0u;
     __syncthreads();
-    uint32_t unused[SORT_PER_THREAD];
-    unsigned fbm;
+    int cur = -1;  // key of the open run (-1: none)
+    uint32_t run = 0u;
+    auto flush = [&]() {
+        if (cur < 0) return;
+        const unsigned w = (unsigned)(cur - k0);
+        if (w < (unsigned)wk)
+            atomicAdd(cnt + w, run);
+        else
+            atomicAdd(A.count + cur, run);
+    };
 #pragma unroll
-    for (int u = 0; u < SUB; ++u) count_keys<false>(A, G, S, k0, Z, keys[u], unused, fbm);
+    for (int j = 0; j < HIST_SEG; ++j) {
+        const int key = c[j] == INT_MIN ? -1 : particle_key(G, A.err, c[j]);
+        if (key != cur) {
+            flush();
+            cur = key;
+            run = 0u;
+        }
+        ++run;
+    }
+    flush();
     __syncthreads();
-    for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
-        const uint32_t v = S.cnt[r];
+    for (int r = threadIdx.x; r < wk; r += SORT_THREADS) {
+        const uint32_t v = cnt[r];
         if (v && k0 + r < A.nkeys) atomicAdd(A.count + k0 + r, v);
     }
-    for (int r = threadIdx.x; r < (1 << Z.hb); r += SORT_THREADS)
-        if (S.hcnt[r]) atomicAdd(A.count + S.hkey[r], S.hcnt[r]);
 }
 
 // Shared memory of a scatter block: the counting state with each key's
