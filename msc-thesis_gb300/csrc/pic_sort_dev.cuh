@@ -279,15 +279,13 @@ __device__ __forceinline__ QuadRuns quad_runs(const int (&k)[SORT_PER_THREAD])
     return R;
 }
 
-// Pass 1 of both kernels: the keys of the thread's quad (`keys` holds its
+// Pass 1 of the scatter: the keys of the thread's quad (`keys` holds its
 // cells on entry; INT_MIN becomes -1) and one shared atomic per run of equal
-// keys (quad_runs), in the window or the table.  With RANK every particle
-// gets its rank among the block's particles of its key: the run's atomic
-// result plus its position in the run.  A run the table has no room for
-// falls back: without RANK its count goes straight to the global histogram,
-// with RANK its particles are marked in `fbm` and take their slots one by
-// one after the reservations.
-template <bool RANK>
+// keys (quad_runs), in the window or the table; every particle gets its rank
+// among the block's particles of its key: the run's atomic result plus its
+// position in the run.  A run the table has no room for falls back: its
+// particles are marked in `fbm` and take their slots one by one after the
+// reservations.
 __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, SortSmem &S,
                                            int k0, SortSizes Z, int (&keys)[SORT_PER_THREAD],
                                            uint32_t (&rank)[SORT_PER_THREAD], unsigned &fbm)
@@ -313,13 +311,11 @@ __device__ __forceinline__ void count_keys(const SortArgs &A, const KeyGeo &G, S
                     base[j] = atomicAdd(S.hcnt + slot, (uint32_t)R.len[j]);
                 } else {
                     fbh[j] = true;
-                    if (!RANK) atomicAdd(A.count + key, (uint32_t)R.len[j]);
                 }
             }
         }
     }
     fbm = 0u;
-    if (!RANK) return;
     // the run entering this lane takes its base and fallback flag from the
     // lane holding its head (that lane's last head)
     const unsigned full = 0xffffffffu;
@@ -468,7 +464,7 @@ __device__ __forceinline__ void sort_scatter_block(const SortArgs &A, const KeyG
     __syncthreads();
     uint32_t rank[SORT_PER_THREAD];
     unsigned fbm;
-    count_keys<true>(A, G, C.s, k0, Z, keys, rank, fbm);
+    count_keys(A, G, C.s, k0, Z, keys, rank, fbm);
     __syncthreads();
     // reserve each distinct key's slice of the output and of the staging order
     for (int r = threadIdx.x; r < Z.wk; r += SORT_THREADS) {
