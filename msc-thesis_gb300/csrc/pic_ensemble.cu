@@ -227,6 +227,7 @@ void ens_free(pic_ensemble *E)
         if (G.c2r) cufftDestroy(G.c2r);
         if (G.r2c2) cufftDestroy(G.r2c2);
         if (G.c2r1) cufftDestroy(G.c2r1);
+        if (G.tw) cudaFree(G.tw);
     }
     if (E->g_one) cudaGraphExecDestroy(E->g_one);
     if (E->g_period) cudaGraphExecDestroy(E->g_period);
@@ -402,6 +403,10 @@ pic_status ens_push_table(pic_ensemble *E, const std::vector<long long> &n_slot)
 
 pic_status ens_plans(pic_ensemble *E)
 {
+    E->spectral = true;
+    for (auto &G : E->groups) E->spectral = E->spectral && spectral_wanted(G.nx, G.ny);
+    if (E->spectral)
+        for (auto &G : E->groups) PIC_TRY(spectral_twiddles(G.nx, G.ny, &G.tw));
     for (auto &G : E->groups) {
         const EnsRun &R = E->runs[G.first];
         // explicit embeddings: with NULL ones cuFFT ignores the batch distances
@@ -474,6 +479,13 @@ pic_status ens_advance(pic_ensemble *E, int kind)
 pic_status ens_poisson(pic_ensemble *E)
 {
     cudaStream_t st = E->stream;
+    if (E->spectral) {
+        for (auto &G : E->groups)
+            PIC_TRY(launch_spectral_runs(E->d_runs, G.first, G.count, G.nx, G.ny, E->rho_fix,
+                                         E->rho, E->rhohat, E->ehat, E->e, G.tw, E->dev, st));
+        PIC_CUDA(cudaMemsetAsync(E->rho_fix, 0, sizeof(unsigned long long) * (size_t)E->nnodes, st));
+        return ens_advance(E, ADV_FIELD);
+    }
     ens_convert_kernel<<<E->nnode_blk, 256, 0, st>>>(E->rho_fix, E->rho, E->node_blk, E->d_runs, E->dev);
     PIC_CUDA(cudaGetLastError());
     PIC_CUDA(cudaMemsetAsync(E->rho_fix, 0, sizeof(unsigned long long) * (size_t)E->nnodes, st));

@@ -75,8 +75,12 @@ struct pic_ensemble {
         int nx, ny, first, count;
         cufftHandle r2c = 0, c2r = 0;
         cufftHandle r2c2 = 0, c2r1 = 0;  // adjoint solve (made on first use)
+        float2 *tw = nullptr;            // spectral solve's twiddle tables
     };
     std::vector<Group> groups;
+    // every group's side lengths are powers of two (16..4096): the step's
+    // solve runs in the spectral kernels, one launch of each per group
+    bool spectral = false;
     // graphs
     cudaGraphExec_t g_one = nullptr, g_period = nullptr, g_sortstep = nullptr;
     int since_sort = 0;

@@ -670,9 +670,8 @@ pic_status pic_create(const pic_config *cfg, pic_handle **out)
     H_CUFFT(cufftSetStream(h->plan_c2r1, h->stream));
     // the step's solve: the spectral kernels on power-of-two grids, unless
     // PIC_FIELD_SOLVER=cufft asks for the library transforms
-    const char *solver = getenv("PIC_FIELD_SOLVER");
-    h->spectral = spectral_size_ok(g.nx, g.ny) && !(solver && strcmp(solver, "cufft") == 0);
-    if (h->spectral) H_TRY(spectral_tables(h));
+    h->spectral = spectral_wanted(g.nx, g.ny);
+    if (h->spectral) H_TRY(spectral_twiddles(g.nx, g.ny, &h->tw));
     H_TRY(reset_device_state(h));
 #undef H_TRY
 #undef H_CUDA

@@ -239,8 +239,17 @@ enum AdvanceKind { ADV_PUSH = 1, ADV_FIELD = 2 };
 pic_status launch_advance(pic_handle *h, int kind);
 // pic_spectral.cu
 bool spectral_size_ok(int nx, int ny);
-pic_status spectral_tables(pic_handle *h);
+// spectral_size_ok, unless the environment variable PIC_FIELD_SOLVER=cufft
+bool spectral_wanted(int nx, int ny);
+pic_status spectral_twiddles(int nx, int ny, float2 **tw);  // cudaMalloc'd tables
 pic_status launch_spectral(pic_handle *h);  // convert + solve, rho_fix cleared
+struct EnsRun;
+// convert + solve of runs [first, first + count) of an ensemble's run table
+// (one grid size; grids at each run's offsets); rho_fix is not cleared
+pic_status launch_spectral_runs(const EnsRun *runs, int first, int count, int nx, int ny,
+                                const unsigned long long *rho_fix, float *rho, float2 *rhohat,
+                                float2 *ehat, float *e, const float2 *tw, DevState *devs,
+                                cudaStream_t st);
 // pic_sort.cu
 pic_status launch_sort(pic_handle *h, int s, bool counts_kept = false);
 pic_status launch_recount(pic_handle *h, int s);

@@ -25,9 +25,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
+#include "pic_ensemble.cuh"
 #include "pic_fft_dev.cuh"
 #include "pic_field_dev.cuh"
 
@@ -48,7 +51,36 @@ struct SpecArgs {
     int pairs, cols, rows;  // row pairs, columns, rows per block of the three kernels
     int sa, sb, sc;         // buffer strides (float2) of the three kernels
     DevState *dev;
+    // ensemble: blockIdx.y picks run first + blockIdx.y of this table, whose
+    // grids sit at its offsets from the pointers above and whose constants
+    // replace the ones above (nullptr: a single run)
+    const EnsRun *runs;
+    int first;
 };
+
+// the arguments of this block's run
+__device__ __forceinline__ SpecArgs block_args(const SpecArgs &P)
+{
+    SpecArgs A = P;
+    if (P.runs) {
+        const int r = P.first + (int)blockIdx.y;
+        const EnsRun &R = P.runs[r];
+        A.rho_fix = P.rho_fix + R.goff;
+        A.rho = P.rho + R.goff;
+        A.S = P.S + R.khoff;
+        A.Tx = P.Tx + R.khoff;
+        A.Ty = P.Tx + R.khoff + R.nk;
+        A.ex = P.ex + 2 * R.goff;
+        A.ey = P.ex + 2 * R.goff + R.ncp;
+        A.mean_fix = R.mean_fix;
+        A.scale = R.rho_scale;
+        A.kx1 = R.kx1;
+        A.ky1 = R.ky1;
+        A.inv_eps0_n = R.inv_eps0_n;
+        A.dev = P.dev + r;
+    }
+    return A;
+}
 
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) { return warp_sum_u64(v); }
 __device__ __forceinline__ double warp_sum(double v) { return warp_sum_d(v); }
@@ -76,8 +108,9 @@ __device__ __forceinline__ T block_sum(T v, T *part)
 
 // LGX: log2 nx.  Block: `pairs` row pairs, nx/16 threads each.
 template <int LGX>
-__global__ void __launch_bounds__(256) spec_rows_fwd_kernel(SpecArgs A)
+__global__ void __launch_bounds__(256) spec_rows_fwd_kernel(SpecArgs P)
 {
+    const SpecArgs A = block_args(P);
     constexpr int NX = 1 << LGX, TP = NX >> 4;
     extern __shared__ float2 smem[];
     __shared__ unsigned long long s_q[32];
@@ -130,8 +163,9 @@ __global__ void __launch_bounds__(256) spec_rows_fwd_kernel(SpecArgs A)
 // LGY: log2 ny.  Block: `cols` columns, ny/16 threads each; two buffers per
 // column (phi^, then Ey^).
 template <int LGY>
-__global__ void __launch_bounds__(256, 2) spec_cols_kernel(SpecArgs A)
+__global__ void __launch_bounds__(256, 2) spec_cols_kernel(SpecArgs P)
 {
+    const SpecArgs A = block_args(P);
     constexpr int NY = 1 << LGY, TP = NY >> 4;
     extern __shared__ float2 smem[];
     __shared__ double s_fe[32];
@@ -196,8 +230,9 @@ __global__ void __launch_bounds__(256, 2) spec_cols_kernel(SpecArgs A)
 
 // LGX: log2 nx.  Block: `rows` rows, nx/16 threads each.
 template <int LGX>
-__global__ void __launch_bounds__(256) spec_rows_inv_kernel(SpecArgs A)
+__global__ void __launch_bounds__(256) spec_rows_inv_kernel(SpecArgs P)
 {
+    const SpecArgs A = block_args(P);
     constexpr int NX = 1 << LGX, TP = NX >> 4, HALF = NX >> 1;
     extern __shared__ float2 smem[];
     const int f = threadIdx.x / TP, t = threadIdx.x - f * TP;
@@ -259,6 +294,12 @@ bool spectral_size_ok(int nx, int ny)
     return ok(nx) && ok(ny);
 }
 
+bool spectral_wanted(int nx, int ny)
+{
+    const char *solver = getenv("PIC_FIELD_SOLVER");
+    return spectral_size_ok(nx, ny) && !(solver && strcmp(solver, "cufft") == 0);
+}
+
 // the transforms' per-pass twiddle tables (fft::twiddle_len entries for nx,
 // then for ny): pass (lgns, lgr) with lgns > 0 holds W_(Ns R)^(r m) at
 // r Ns + m, r < R, m < Ns
@@ -276,51 +317,33 @@ static void append_twiddles(std::vector<float2> &t, int lgn)
     }
 }
 
-pic_status spectral_tables(pic_handle *h)
+pic_status spectral_twiddles(int nx, int ny, float2 **tw)
 {
     std::vector<float2> t;
-    append_twiddles(t, ilog2(h->g.nx));
-    append_twiddles(t, ilog2(h->g.ny));
+    append_twiddles(t, ilog2(nx));
+    append_twiddles(t, ilog2(ny));
     t.push_back(make_float2(1.f, 0.f));  // never empty (16-point transforms need none)
-    PIC_CUDA(cudaMalloc(&h->tw, t.size() * sizeof(float2)));
-    PIC_CUDA(cudaMemcpy(h->tw, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    PIC_CUDA(cudaMalloc(tw, t.size() * sizeof(float2)));
+    PIC_CUDA(cudaMemcpy(*tw, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice));
     return PIC_OK;
 }
 
-pic_status launch_spectral(pic_handle *h)
+// The three kernels over `batch` runs of one grid size (A.runs set) or one
+// run.  The caller clears the fixed-point density afterwards.
+static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st)
 {
-    const Geometry &g = h->g;
-    SpecArgs A;
-    A.rho_fix = h->rho_fix;
-    A.rho = h->rho;
-    A.S = h->rhohat;
-    A.Tx = h->ehat;
-    A.Ty = h->ehat + (size_t)g.nh * g.ny;
-    A.ex = h->e;
-    A.ey = h->e + (size_t)g.nx * g.ny;
-    A.nx = g.nx;
-    A.ny = g.ny;
-    A.nh = g.nh;
-    A.lgx = ilog2(g.nx);
-    A.lgy = ilog2(g.ny);
-    A.twx = h->tw;
-    A.twy = h->tw + fft::twiddle_len(A.lgx);
-    A.mean_fix = h->mean_fix;
-    A.scale = (float)(h->q_unit / (4294967296.0 * g.dx * g.dy));
-    A.kx1 = (float)(2.0 * 3.14159265358979323846 / g.Lx);
-    A.ky1 = (float)(2.0 * 3.14159265358979323846 / g.Ly);
-    A.inv_eps0_n = (float)(1.0 / (h->cfg.eps0 * (double)g.nx * (double)g.ny));
-    A.tmx = h->track_mx;
-    A.tmy = h->track_my;
-    A.dev = h->dev;
-    const int tpx = g.nx >> 4, tpy = g.ny >> 4;
-    A.pairs = std::max(1, std::min(256 / tpx, g.ny / 2));
+    const int nx = A.nx, ny = A.ny, nh = A.nh;
+    A.lgx = ilog2(nx);
+    A.lgy = ilog2(ny);
+    A.twy = A.twx + fft::twiddle_len(A.lgx);
+    const int tpx = nx >> 4, tpy = ny >> 4;
+    A.pairs = std::max(1, std::min(256 / tpx, ny / 2));
     A.cols = std::max(1, 256 / tpy);
-    A.rows = std::max(1, std::min(256 / tpx, g.ny));
+    A.rows = std::max(1, std::min(256 / tpx, ny));
     // interleaved buffers read by consecutive lanes start on different banks
-    A.sa = fft::buf_stride(g.nx, 16 / std::min(A.pairs, 16));
-    A.sb = fft::buf_stride(g.ny, 8);
-    A.sc = fft::buf_stride(g.nx, 16 / std::min(A.rows, 16));
+    A.sa = fft::buf_stride(nx, 16 / std::min(A.pairs, 16));
+    A.sb = fft::buf_stride(ny, 8);
+    A.sc = fft::buf_stride(nx, 16 / std::min(A.rows, 16));
     const size_t ma = (size_t)A.pairs * A.sa * sizeof(float2);
     const size_t mb = (size_t)2 * A.cols * A.sb * sizeof(float2);
     const size_t mc = (size_t)A.rows * A.sc * sizeof(float2);
@@ -342,7 +365,7 @@ pic_status launch_spectral(pic_handle *h)
         PIC_SPEC_Y(10) PIC_SPEC_Y(11) PIC_SPEC_Y(12)
 #undef PIC_SPEC_Y
     }
-    if (!ka || !kb) {
+    if (!ka || !kb || batch < 1) {
         set_error("spectral solve: grid side outside 16..4096");
         return PIC_ERR_INVALID_ARG;
     }
@@ -350,13 +373,65 @@ pic_status launch_spectral(pic_handle *h)
     PIC_TRY(allow_dynamic_smem(kb, mb));
     PIC_TRY(allow_dynamic_smem(kc, mc));
     void *args[] = {&A};
-    PIC_CUDA(cudaLaunchKernel(ka, dim3(g.ny / (2 * A.pairs)), dim3(A.pairs * tpx), args, ma, h->stream));
+    const unsigned nb = (unsigned)batch;
+    PIC_CUDA(cudaLaunchKernel(ka, dim3(ny / (2 * A.pairs), nb), dim3(A.pairs * tpx), args, ma, st));
+    PIC_CUDA(cudaLaunchKernel(kb, dim3((nh + A.cols - 1) / A.cols, nb), dim3(A.cols * tpy), args,
+                              mb, st));
+    PIC_CUDA(cudaLaunchKernel(kc, dim3(ny / A.rows, nb), dim3(A.rows * tpx), args, mc, st));
+    return PIC_OK;
+}
+
+pic_status launch_spectral(pic_handle *h)
+{
+    const Geometry &g = h->g;
+    SpecArgs A;
+    memset(&A, 0, sizeof A);
+    A.rho_fix = h->rho_fix;
+    A.rho = h->rho;
+    A.S = h->rhohat;
+    A.Tx = h->ehat;
+    A.Ty = h->ehat + (size_t)g.nh * g.ny;
+    A.ex = h->e;
+    A.ey = h->e + (size_t)g.nx * g.ny;
+    A.nx = g.nx;
+    A.ny = g.ny;
+    A.nh = g.nh;
+    A.twx = h->tw;
+    A.mean_fix = h->mean_fix;
+    A.scale = (float)(h->q_unit / (4294967296.0 * g.dx * g.dy));
+    A.kx1 = (float)(2.0 * 3.14159265358979323846 / g.Lx);
+    A.ky1 = (float)(2.0 * 3.14159265358979323846 / g.Ly);
+    A.inv_eps0_n = (float)(1.0 / (h->cfg.eps0 * (double)g.nx * (double)g.ny));
+    A.tmx = h->track_mx;
+    A.tmy = h->track_my;
+    A.dev = h->dev;
+    PIC_TRY(launch_kernels(A, 1, h->stream));
     PIC_CUDA(cudaMemsetAsync(h->rho_fix, 0, sizeof(unsigned long long) * (size_t)g.nx * g.ny,
                              h->stream));
-    PIC_CUDA(cudaLaunchKernel(kb, dim3((g.nh + A.cols - 1) / A.cols), dim3(A.cols * tpy), args, mb,
-                              h->stream));
-    PIC_CUDA(cudaLaunchKernel(kc, dim3(g.ny / A.rows), dim3(A.rows * tpx), args, mc, h->stream));
     return PIC_OK;
+}
+
+pic_status launch_spectral_runs(const EnsRun *runs, int first, int count, int nx, int ny,
+                                const unsigned long long *rho_fix, float *rho, float2 *rhohat,
+                                float2 *ehat, float *e, const float2 *tw, DevState *devs,
+                                cudaStream_t st)
+{
+    SpecArgs A;
+    memset(&A, 0, sizeof A);
+    A.rho_fix = rho_fix;
+    A.rho = rho;
+    A.S = rhohat;
+    A.Tx = ehat;
+    A.ex = e;
+    A.nx = nx;
+    A.ny = ny;
+    A.nh = nx / 2 + 1;
+    A.twx = tw;
+    A.tmx = A.tmy = -1;
+    A.dev = devs;
+    A.runs = runs;
+    A.first = first;
+    return launch_kernels(A, count, st);
 }
 
 }  // namespace pic

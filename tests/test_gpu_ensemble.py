@@ -1,5 +1,7 @@
 """Ensembles (pic_ensemble_*) against the same runs on single handles and
 against the FP64 oracle."""
+import os
+
 import numpy as np
 import pytest
 
@@ -61,6 +63,9 @@ def test_ensemble_runs_match_single_handles():
         exact += same
         print(f"run {r}: {cfg.nx}x{cfg.ny}, max position difference {err:.2e} cells, "
               f"bit-identical {same}, FE rel diff {np.max(np.abs(fe_ens[r] - fe) / fe.max()):.2e}")
+        # power-of-two grids: the ensemble and the single handle solve with the
+        # same spectral kernels, run by run, so the particles agree bit for bit
+        assert same
         assert err < 1e-4
         np.testing.assert_allclose(ens[r]["vx"], a["vx"], atol=1e-5)
         np.testing.assert_allclose(fe_ens[r], fe, rtol=1e-5, atol=1e-6 * fe.max())
@@ -82,6 +87,56 @@ def test_ensemble_independent_of_sort_cadence():
     for r in range(3):
         for k in out[0][r]:
             np.testing.assert_array_equal(out[0][r][k], out[1][r][k], err_msg=f"run {r} {k}")
+
+
+def ensemble_run(runs, nst, solver=None):
+    cfgs, specs = build(runs, sort_every=5, chunk=1024)
+    old = os.environ.get("PIC_FIELD_SOLVER")
+    if solver:
+        os.environ["PIC_FIELD_SOLVER"] = solver
+    try:
+        with P.Ensemble(cfgs) as E:
+            E.init(specs)
+            E.step(nst)
+            E.synchronize()
+            parts = [E.get_particles(r) for r in range(len(runs))]
+            fe = [E.history(r, P.HIST_FIELD_ENERGY, 0, nst + 1) for r in range(len(runs))]
+    finally:
+        if old is None:
+            os.environ.pop("PIC_FIELD_SOLVER", None)
+        else:
+            os.environ["PIC_FIELD_SOLVER"] = old
+    return cfgs, parts, fe
+
+
+def test_ensemble_cufft_path_matches_spectral_path():
+    """The ensemble's cuFFT solve (grids that are not powers of two, or
+    PIC_FIELD_SOLVER=cufft) against its spectral solve on the same runs, and
+    an ensemble with a 48 x 32 run (cuFFT for every group) against single
+    handles."""
+    nst = 20
+    cfgs, a, fa = ensemble_run(RUNS[:3], nst)
+    _, b, fb = ensemble_run(RUNS[:3], nst, "cufft")
+    for r, cfg in enumerate(cfgs):
+        err = max(np.abs(periodic_diff(a[r]["x"], b[r]["x"], L)).max(),
+                  np.abs(periodic_diff(a[r]["y"], b[r]["y"], L)).max()) / (L / cfg.nx)
+        rel = np.abs(fa[r] - fb[r]).max() / fb[r].max()
+        print(f"run {r}: spectral vs cuFFT, positions {err:.2e} cells, FE {rel:.2e}")
+        assert err < 1e-4 and rel < 1e-5
+    mixed = [(48, 32, 16, 0.2, 1e-3, 21), (32, 32, 16, 0.15, 1e-3, 22)]
+    cfgs, e, fe = ensemble_run(mixed, nst)
+    for r, (cfg, spec) in enumerate(zip(*build(mixed, sort_every=5, chunk=1024))):
+        with P.Handle(cfg) as h:
+            h.init_particles(0, spec)
+            h.prime_leapfrog()
+            h.step(nst)
+            s = h.get_particles(0)
+            fs = h.history(P.HIST_FIELD_ENERGY, 0, nst + 1)
+        err = max(np.abs(periodic_diff(e[r]["x"], s["x"], L)).max(),
+                  np.abs(periodic_diff(e[r]["y"], s["y"], L)).max()) / (L / cfg.nx)
+        rel = np.abs(fe[r] - fs).max() / fs.max()
+        print(f"mixed run {r} ({cfg.nx}x{cfg.ny}): vs single handle {err:.2e} cells, FE {rel:.2e}")
+        assert err < 1e-4 and rel < 1e-5
 
 
 @pytest.mark.parametrize("runs,nst,bar", [
