@@ -281,6 +281,13 @@ __global__ void __launch_bounds__(256) spec_rows_inv_kernel(SpecArgs P)
     }
 }
 
+static int pow2_floor(int n)
+{
+    int p = 1;
+    while (2 * p <= n) p *= 2;
+    return p;
+}
+
 static int ilog2(int n)
 {
     int l = 0;
@@ -337,9 +344,19 @@ static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st)
     A.lgy = ilog2(ny);
     A.twy = A.twx + fft::twiddle_len(A.lgx);
     const int tpx = nx >> 4, tpy = ny >> 4;
-    A.pairs = std::max(1, std::min(256 / tpx, ny / 2));
-    A.cols = std::max(1, 256 / tpy);
-    A.rows = std::max(1, std::min(256 / tpx, ny));
+    // transforms per block: at most 256 threads, and no more than spreads the
+    // batch's transforms over about one block per SM (small grids otherwise
+    // run on a few SMs), but at least a warp's worth where the grid allows
+    const int sms = device_sms();
+    auto per_block = [&](int tp, int items) {
+        const int spread = (int)std::max(1ll, (long long)items * batch / sms);
+        int k = std::min(256 / tp, pow2_floor(spread));
+        k = std::max(k, std::min(32 / tp, items));
+        return std::max(1, std::min(k, items));
+    };
+    A.pairs = per_block(tpx, ny / 2);
+    A.cols = per_block(tpy, nh);
+    A.rows = per_block(tpx, ny);
     // interleaved buffers read by consecutive lanes start on different banks
     A.sa = fft::buf_stride(nx, 16 / std::min(A.pairs, 16));
     A.sb = fft::buf_stride(ny, 8);
