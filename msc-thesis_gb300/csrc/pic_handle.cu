@@ -200,10 +200,13 @@ static pic_status setup_geometry(pic_handle *h)
     g.dx = c.Lx / c.nx;
     g.dy = c.Ly / c.ny;
     g.chunk = c.chunk ? c.chunk : 8192;
-    // default halo 4 cells (measured at 2048^2 x 32 ppc, sort every 40: 1.203
-    // ms per step against 1.234 with 2, 1.211 with 5 or 6, 1.300 with 8),
-    // less where the window would not fit
-    g.halo = c.halo ? c.halo : 4;
+    // default halo: the particles' drift between sorts grows with the cadence
+    // (2048^2 x 32 ppc, sort every 40: 1.203 ms per step with 4 cells against
+    // 1.234 with 2, 1.216 with 3, 1.211 with 5 or 6, 1.300 with 8; sort every
+    // 20: 1.100 ms with 3 against 1.106 with 4), less where the window would
+    // not fit
+    const int every = c.sort_every ? c.sort_every : 20;
+    g.halo = c.halo ? c.halo : (every <= 20 ? 3 : 4);
     long long maxcap = 0;
     for (int s = 0; s < c.nspecies; ++s) maxcap = std::max(maxcap, c.species[s].capacity);
     const double ppc = std::max(1.0, (double)maxcap / ((double)c.nx * c.ny));
