@@ -342,7 +342,13 @@ static pic_status sort_now(pic_handle *h, bool import = false)
         for (int s = 0; s < h->cfg.nspecies; ++s) {
             if (!h->sp[s].cap || first[s] != (pass == 0)) continue;
             bool in0 = false;
-            PIC_TRY(import ? import_sort(h, s, &in0) : launch_sort(h, s));
+            if (import && h->sp[s].presorted) {  // sorted range by range on the way in
+                h->sp[s].presorted = false;
+                in0 = true;
+                PIC_TRY(launch_anchors(h, s, 0));
+            } else {
+                PIC_TRY(import ? import_sort(h, s, &in0) : launch_sort(h, s));
+            }
             if (!in0) PIC_TRY(copy_back(h, s));
             if (import) PIC_TRY(launch_recount(h, s));  // the DSMC species' kept counts
         }
@@ -750,6 +756,17 @@ pic_status pic_init_particles(pic_handle *h, int s, const pic_init_spec *spec)
     return refresh(h);
 }
 
+// The handle's second stream and its events (export copies, import ranges),
+// created on first use.
+pic_status pic::ensure_copy_stream(pic_handle *h)
+{
+    if (h->copy_stream) return PIC_OK;
+    PIC_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (auto &e : h->field_ready) PIC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PIC_CUDA(cudaEventCreateWithFlags(&h->copies_done, cudaEventDisableTiming));
+    return PIC_OK;
+}
+
 pic_status pic_set_particles(pic_handle *h, int s, long long n, const double *x, const double *y,
                              const double *vx, const double *vy, const double *vz)
 {
@@ -769,8 +786,12 @@ pic_status pic_set_particles(pic_handle *h, int s, long long n, const double *x,
         const size_t rec_bytes = (size_t)h->sp[s].cap * 48;
         if (stage_fits(h, rec_bytes)) {
             PIC_TRY(ensure_stage(h, rec_bytes));
-            PIC_TRY(launch_from_global_records(h, s, n, dx, dy, dvx, dvy, dvz));
-            h->sp[s].records_ready = true;
+            if (h->sp[s].cap >= IMPORT_SPLIT_MIN) {
+                PIC_TRY(import_records_in_parts(h, s, n, dx, dy, dvx, dvy, dvz));
+            } else {
+                PIC_TRY(launch_from_global_records(h, s, n, dx, dy, dvx, dvy, dvz));
+                h->sp[s].records_ready = true;
+            }
         } else {
             PIC_TRY(launch_from_global(h, s, n, dx, dy, dvx, dvy, dvz));
         }
@@ -790,6 +811,7 @@ pic_status pic_set_particles(pic_handle *h, int s, long long n, const double *x,
     pic_status rc = reset_device_state(h);
     if (rc == PIC_OK) rc = refresh(h);
     h->sp[s].records_ready = false;  // consumed by the import sort, or stale after an error
+    h->sp[s].presorted = false;
     return rc;
 }
 
@@ -823,11 +845,7 @@ pic_status pic_get_particles(pic_handle *h, int s, long long *n, double *x, doub
     uint4 *rec = (uint4 *)h->stage;
     double *d = packed ? (double *)(rec + 2 * part_max) : (double *)h->stage;
     uint32_t *inv = (uint32_t *)(d + nreq * nn);
-    if (!h->copy_stream) {
-        PIC_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
-        for (auto &e : h->field_ready) PIC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        PIC_CUDA(cudaEventCreateWithFlags(&h->copies_done, cudaEventDisableTiming));
-    }
+    PIC_TRY(ensure_copy_stream(h));
     double *dev[5];
     for (int k = 0, j = 0; k < 5; ++k) dev[k] = host[k] ? d + (j++) * nn : nullptr;
     if (packed) {

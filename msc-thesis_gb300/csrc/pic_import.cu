@@ -12,6 +12,7 @@
 // per import, never in the step.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include <cub/device/device_radix_sort.cuh>
@@ -196,6 +197,76 @@ pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
     PIC_CUDA(cudaGetLastError());
     *in_buffer0 = packed;
     return launch_anchors(h, s, ob);
+}
+
+// Page-locked host arrays of species s (n live particles of its cap slots)
+// into buffer 0, in key order within each of IMPORT_PARTS slot ranges: the
+// conversion kernel reads range k over the link on the handle's stream
+// while range k - 1 is radix-sorted and unpacked on the copy stream, so
+// that only the last range's sort follows the transfer.  The push needs no
+// more than ranges in key order (a push chunk lies in one range but for the
+// few that straddle two, which take the push's global path), and the next
+// periodic sort orders the whole array.
+pic_status import_records_in_parts(pic_handle *h, int s, long long n, const double *x_dev,
+                                   const double *y_dev, const double *vx_dev,
+                                   const double *vy_dev, const double *vz_dev)
+{
+    SpeciesBuf &B = h->sp[s];
+    const long long cap = B.cap;
+    if (cap >= (1ll << 31)) {
+        set_error("import sort: more than 2^31 slots");
+        return PIC_ERR_INVALID_ARG;
+    }
+    PIC_TRY(ensure_copy_stream(h));
+    const Geometry &g = h->g;
+    const int bits = key_bits((long long)g.nx * g.ny + 1);
+    uint32_t *scratch = (uint32_t *)h->stage;
+    const uint4 *rec = reinterpret_cast<const uint4 *>(scratch + 4 * cap);
+    long long bnd[IMPORT_PARTS + 1];
+    for (int k = 0; k < IMPORT_PARTS; ++k) bnd[k] = ((cap * k / IMPORT_PARTS) + 3) & ~3ll;
+    bnd[IMPORT_PARTS] = cap;
+    // CUB's temporary storage for the largest range, allocated before the
+    // first range is converted (an allocation would wait for the device)
+    size_t need = 0;
+    for (int k = 0; k < IMPORT_PARTS; ++k) {
+        cub::DoubleBuffer<uint32_t> kk(scratch, scratch + cap), vv(scratch + 2 * cap, scratch + 3 * cap);
+        size_t b = 0;
+        PIC_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, b, kk, vv, (int)(bnd[k + 1] - bnd[k]), 0,
+                                                 bits, h->copy_stream));
+        need = std::max(need, b);
+    }
+    if (need > h->cub_temp_bytes) {
+        if (h->cub_temp) cudaFree(h->cub_temp);
+        h->cub_temp = nullptr;
+        h->cub_temp_bytes = 0;
+        PIC_CUDA(cudaMalloc(&h->cub_temp, need));
+        h->cub_temp_bytes = need;
+    }
+    void *out[7] = {B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.pid[0], B.vz[0]};
+    const int nf = B.vz[0] ? 7 : 6;
+    for (int k = 0; k < IMPORT_PARTS; ++k) {
+        const long long lo = bnd[k], m = bnd[k + 1] - bnd[k];
+        if (m <= 0) continue;
+        PIC_TRY(launch_from_global_records_range(h, s, n, lo, lo + m, x_dev, y_dev, vx_dev, vy_dev,
+                                                 vz_dev));
+        PIC_CUDA(cudaEventRecord(h->field_ready[k], h->stream));
+        PIC_CUDA(cudaStreamWaitEvent(h->copy_stream, h->field_ready[k], 0));
+        cub::DoubleBuffer<uint32_t> keys(scratch + lo, scratch + cap + lo),
+            vals(scratch + 2 * cap + lo, scratch + 3 * cap + lo);
+        size_t tb = h->cub_temp_bytes;
+        PIC_CUDA(cub::DeviceRadixSort::SortPairs(h->cub_temp, tb, keys, vals, (int)m, 0, bits,
+                                                 h->copy_stream));
+        Fields F;
+        memset(&F, 0, sizeof F);
+        F.nf = nf;
+        for (int f = 0; f < nf; ++f) F.out[f] = (uint32_t *)out[f] + lo;
+        import_unpack_kernel<<<grid_for(m, 256), 256, 0, h->copy_stream>>>(F, rec, vals.Current(), m);
+        PIC_CUDA(cudaGetLastError());
+    }
+    PIC_CUDA(cudaEventRecord(h->copies_done, h->copy_stream));
+    PIC_CUDA(cudaStreamWaitEvent(h->stream, h->copies_done, 0));
+    B.presorted = true;
+    return PIC_OK;
 }
 
 // Every run of an ensemble: buffer 0 in arbitrary order -> buffer 1 in key

@@ -124,17 +124,19 @@ __global__ void from_global_kernel(InitArgs A, const double *x, const double *y,
     }
 }
 
-// Host arrays straight to the import sort's input: for every slot its key
-// and slot number, and its fields as the 32-byte record {cell, ox, oy, vx},
-// {vy, pid, vz, 0}; slots n..cap-1 are empty (cell -1, the empty key).
-__global__ void from_global_records_kernel(InitArgs A, KeyGeo G, long long cap, unsigned *err,
+// Host arrays straight to the import sort's input: for every slot of
+// [lo, hi) its key and slot number, and its fields as the 32-byte record
+// {cell, ox, oy, vx}, {vy, pid, vz, 0}; slots n..cap-1 are empty (cell -1,
+// the empty key).
+__global__ void from_global_records_kernel(InitArgs A, KeyGeo G, long long lo, long long hi,
+                                           unsigned *err,
                                            const double *x, const double *y, const double *vx,
                                            const double *vy, const double *vz,
                                            uint32_t *__restrict__ keys, uint32_t *__restrict__ idx,
                                            uint4 *__restrict__ rec)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
+    for (long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += stride) {
         idx[i] = (uint32_t)i;
         if (i < A.n) {
             int cx, cy;
@@ -426,23 +428,35 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
     return PIC_OK;
 }
 
-pic_status launch_from_global_records(pic_handle *h, int s, long long n, const double *x_dev,
-                                      const double *y_dev, const double *vx_dev,
-                                      const double *vy_dev, const double *vz_dev)
+// Slots [lo, hi) of species s from device-visible host arrays into the stage
+// (keys, slots and records laid out for a cap-slot import sort), on the
+// handle's stream.
+pic_status launch_from_global_records_range(pic_handle *h, int s, long long n, long long lo,
+                                            long long hi, const double *x_dev, const double *y_dev,
+                                            const double *vx_dev, const double *vy_dev,
+                                            const double *vz_dev)
 {
     SpeciesBuf &B = h->sp[s];
     const long long cap = B.cap;
-    if (!cap) return PIC_OK;
+    if (!cap || hi <= lo) return PIC_OK;
     InitArgs A = base_args(h, s);
     A.n = n;
     const Geometry &g = h->g;
     const KeyGeo G = key_geo(g.nx, g.ny, g.tw, g.th, g.ntx, 0);
     uint32_t *scratch = (uint32_t *)h->stage;
-    from_global_records_kernel<<<grid_for(cap, 256), 256, 0, h->stream>>>(
-        A, G, cap, &h->dev->err, x_dev, y_dev, vx_dev, vy_dev, vz_dev, scratch, scratch + 2 * cap,
-        reinterpret_cast<uint4 *>(scratch + 4 * cap));
+    from_global_records_kernel<<<grid_for(hi - lo, 256), 256, 0, h->stream>>>(
+        A, G, lo, hi, &h->dev->err, x_dev, y_dev, vx_dev, vy_dev, vz_dev, scratch,
+        scratch + 2 * cap, reinterpret_cast<uint4 *>(scratch + 4 * cap));
     PIC_CUDA(cudaGetLastError());
     return PIC_OK;
+}
+
+pic_status launch_from_global_records(pic_handle *h, int s, long long n, const double *x_dev,
+                                      const double *y_dev, const double *vx_dev,
+                                      const double *vy_dev, const double *vz_dev)
+{
+    return launch_from_global_records_range(h, s, n, 0, h->sp[s].cap, x_dev, y_dev, vx_dev,
+                                            vy_dev, vz_dev);
 }
 
 // Export of species s in id order into five device arrays out[0..4] (x, y,

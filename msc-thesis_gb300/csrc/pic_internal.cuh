@@ -118,7 +118,14 @@ struct SpeciesBuf {
     long long n = 0;            // host mirror of the count
     long long nchunks = 0;      // push grid size for this species
     bool records_ready = false; // import keys and records already in the stage
+    bool presorted = false;     // imported already sorted, range by range
 };
+
+// An import from page-locked host arrays of at least IMPORT_SPLIT_MIN slots
+// is converted and radix-sorted in IMPORT_PARTS slot ranges, each range
+// sorted on the copy stream while the next one crosses the link.
+constexpr int IMPORT_PARTS = 8;
+constexpr long long IMPORT_SPLIT_MIN = 1ll << 22;
 
 // An export of at least EXPORT_SPLIT_MIN particles is done in EXPORT_PARTS
 // id ranges, each copied to the host while the next one is prepared.
@@ -259,6 +266,10 @@ pic_status launch_anchors(pic_handle *h, int s, int buf = 1);
 // pic_import.cu: arbitrary order in buffer 0 -> key order in buffer 0 (records)
 // or buffer 1 (per-field gather), with the anchors
 pic_status import_sort(pic_handle *h, int s, bool *in_buffer0);
+pic_status import_records_in_parts(pic_handle *h, int s, long long n, const double *x_dev,
+                                   const double *y_dev, const double *vx_dev,
+                                   const double *vy_dev, const double *vz_dev);
+pic_status ensure_copy_stream(pic_handle *h);
 // exclusive scan of count[0, nkeys) into offset and cursor, offset[nkeys] =
 // *d_total; bsum, bsum_s: ceil(nkeys / 4096) entries, bsum2: ceil(that / 4096)
 pic_status launch_key_scan(const uint32_t *count, uint32_t *offset, uint32_t *cursor,
@@ -274,6 +285,10 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
                               const double *vz_dev);
 // the same conversion straight into the import sort's stage layout (keys,
 // slots and packed records of all cap slots; see import_sort)
+pic_status launch_from_global_records_range(pic_handle *h, int s, long long n, long long lo,
+                                            long long hi, const double *x_dev, const double *y_dev,
+                                            const double *vx_dev, const double *vy_dev,
+                                            const double *vz_dev);
 pic_status launch_from_global_records(pic_handle *h, int s, long long n, const double *x_dev,
                                       const double *y_dev, const double *vx_dev,
                                       const double *vy_dev, const double *vz_dev);

@@ -130,3 +130,55 @@ def test_empty_single_and_full_imports(lean):
             os.environ.pop("PIC_STAGE_MAX_BYTES", None)
         else:
             os.environ["PIC_STAGE_MAX_BYTES"] = old
+
+
+@pytest.mark.parametrize("vz", [False, True])
+def test_large_import_sorted_range_by_range(vz):
+    """From 2^22 slots an import from page-locked arrays is converted and
+    radix-sorted in eight slot ranges, each range's sort overlapping the next
+    range's transfer: every range is in tile-major cell-key order and the
+    particles are the same as through the whole-array sort of the per-field
+    path, before and after steps that include a periodic sort."""
+    nx, ny, tw, th = 256, 192, 16, 8
+    n = (1 << 22) + 7
+    arrs = _particles(n, 14, vz)
+    out = {}
+    for lean in (False, True):
+        old = os.environ.get("PIC_STAGE_MAX_BYTES")
+        if lean:
+            os.environ["PIC_STAGE_MAX_BYTES"] = "1"
+        try:
+            cfg, q, m = normalized_electrons(nx, ny, 8.0, 6.0, n, 0.05, sort_every=7,
+                                             tile_w=tw, tile_h=th)
+            cfg.species[0] = P.species(n + 37, q, m, -1, P.SPECIES_HAS_VZ if vz else 0)
+            src = [torch.from_numpy(a).pin_memory().numpy() for a in arrs]
+            with P.Handle(cfg) as h:
+                h.set_particles(0, *src)
+                raw = h.get_particles_raw(0)
+                first = h.get_particles(0, vz=vz)
+                h.prime_leapfrog()
+                h.step(9)
+                d = h.diagnostics()
+                assert d.error_flags == 0 and d.total_charge_fixed == d.expected_charge_fixed
+                out[lean] = (raw, first, h.get_particles(0, vz=vz), d.field_energy)
+        finally:
+            if old is None:
+                os.environ.pop("PIC_STAGE_MAX_BYTES", None)
+            else:
+                os.environ["PIC_STAGE_MAX_BYTES"] = old
+    raw = out[False][0]
+    cell = raw["cell"][:n]
+    cx, cy = cell & 0xFFFF, cell >> 16
+    ntx = nx // tw
+    key = (((cy // th) * ntx + cx // tw) * th + cy % th) * tw + cx % tw
+    cap = (n + 37 + 3) & ~3
+    bnd = [((cap * k // 8) + 3) & ~3 for k in range(8)] + [cap]
+    for k in range(8):
+        seg = key[bnd[k]:min(bnd[k + 1], n)]
+        assert np.all(np.diff(seg) >= 0), k
+    assert np.count_nonzero(np.diff(key) < 0) >= 1  # ranges, not one sorted array
+    assert np.array_equal(np.sort(raw["pid"][:n]), np.arange(n, dtype=np.uint32))
+    for k in out[False][1]:
+        np.testing.assert_array_equal(out[False][1][k], out[True][1][k], err_msg="import " + k)
+        np.testing.assert_array_equal(out[False][2][k], out[True][2][k], err_msg="after steps " + k)
+    assert out[False][3] == out[True][3]
