@@ -536,6 +536,17 @@ pic_status lattice_dims(pic_handle *h, long long n, int *lx, int *ly)
     return lattice_dims_for(h->g.nx, h->g.ny, n, lx, ly);
 }
 
+// The handle's second stream and its events (export copies, import ranges),
+// created on first use.
+pic_status ensure_copy_stream(pic_handle *h)
+{
+    if (h->copy_stream) return PIC_OK;
+    PIC_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (auto &e : h->field_ready) PIC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PIC_CUDA(cudaEventCreateWithFlags(&h->copies_done, cudaEventDisableTiming));
+    return PIC_OK;
+}
+
 }  // namespace pic
 
 using namespace pic;
@@ -754,17 +765,6 @@ pic_status pic_init_particles(pic_handle *h, int s, const pic_init_spec *spec)
     PIC_TRY(launch_init(h, s, spec, lx, ly));
     PIC_TRY(reset_device_state(h));
     return refresh(h);
-}
-
-// The handle's second stream and its events (export copies, import ranges),
-// created on first use.
-pic_status pic::ensure_copy_stream(pic_handle *h)
-{
-    if (h->copy_stream) return PIC_OK;
-    PIC_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
-    for (auto &e : h->field_ready) PIC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    PIC_CUDA(cudaEventCreateWithFlags(&h->copies_done, cudaEventDisableTiming));
-    return PIC_OK;
 }
 
 pic_status pic_set_particles(pic_handle *h, int s, long long n, const double *x, const double *y,
