@@ -342,10 +342,10 @@ static pic_status sort_now(pic_handle *h, bool import = false)
         for (int s = 0; s < h->cfg.nspecies; ++s) {
             if (!h->sp[s].cap || first[s] != (pass == 0)) continue;
             bool in0 = false;
-            if (import && h->sp[s].presorted) {  // sorted range by range on the way in
+            if (import && h->sp[s].presorted) {  // in buffer 1, sorted range by range
                 h->sp[s].presorted = false;
                 in0 = true;
-                PIC_TRY(launch_anchors(h, s, 0));
+                PIC_TRY(launch_sort(h, s, false, 1));  // one counting sort into buffer 0
             } else {
                 PIC_TRY(import ? import_sort(h, s, &in0) : launch_sort(h, s));
             }

@@ -200,13 +200,14 @@ pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
 }
 
 // Page-locked host arrays of species s (n live particles of its cap slots)
-// into buffer 0, in key order within each of IMPORT_PARTS slot ranges: the
+// into buffer 1, in key order within each of IMPORT_PARTS slot ranges: the
 // conversion kernel reads range k over the link on the handle's stream
 // while range k - 1 is radix-sorted and unpacked on the copy stream, so
-// that only the last range's sort follows the transfer.  The push needs no
-// more than ranges in key order (a push chunk lies in one range but for the
-// few that straddle two, which take the push's global path), and the next
-// periodic sort orders the whole array.
+// that only the last range's sort follows the transfer.  Each range holds
+// particles of the whole grid at an eighth of the density, where a push
+// chunk would span eight tiles, so the caller then runs one counting sort
+// from buffer 1 into buffer 0: cheap on such data, whose every block of
+// particles spans a few cells of one range.
 pic_status import_records_in_parts(pic_handle *h, int s, long long n, const double *x_dev,
                                    const double *y_dev, const double *vx_dev,
                                    const double *vy_dev, const double *vz_dev)
@@ -242,8 +243,8 @@ pic_status import_records_in_parts(pic_handle *h, int s, long long n, const doub
         PIC_CUDA(cudaMalloc(&h->cub_temp, need));
         h->cub_temp_bytes = need;
     }
-    void *out[7] = {B.cell[0], B.ox[0], B.oy[0], B.vx[0], B.vy[0], B.pid[0], B.vz[0]};
-    const int nf = B.vz[0] ? 7 : 6;
+    void *out[7] = {B.cell[1], B.ox[1], B.oy[1], B.vx[1], B.vy[1], B.pid[1], B.vz[1]};
+    const int nf = B.vz[1] ? 7 : 6;
     for (int k = 0; k < IMPORT_PARTS; ++k) {
         const long long lo = bnd[k], m = bnd[k + 1] - bnd[k];
         if (m <= 0) continue;

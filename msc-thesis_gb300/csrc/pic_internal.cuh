@@ -258,7 +258,7 @@ pic_status launch_spectral_runs(const EnsRun *runs, int first, int count, int nx
                                 float2 *ehat, float *e, const float2 *tw, DevState *devs,
                                 cudaStream_t st);
 // pic_sort.cu
-pic_status launch_sort(pic_handle *h, int s, bool counts_kept = false);
+pic_status launch_sort(pic_handle *h, int s, bool counts_kept = false, int from = 0);
 pic_status launch_recount(pic_handle *h, int s);
 void sort_sizes_for(double density, int *wk, int *hb);
 pic_status scatter_smem_attr(const void *kernel);

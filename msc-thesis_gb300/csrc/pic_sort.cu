@@ -264,27 +264,28 @@ void sort_sizes_for(double density, int *wk, int *hb)
 
 // Arguments of a sort of species s from buffer 0 into buffer 1.  The DSMC
 // species counts into its own array (kept current by its pushes).
-static SortArgs sort_args(pic_handle *h, int s)
+static SortArgs sort_args(pic_handle *h, int s, int from = 0)
 {
     SpeciesBuf &B = h->sp[s];
     const Geometry &g = h->g;
     const long long ncell = (long long)g.nx * g.ny;
     SortArgs A;
     memset(&A, 0, sizeof A);
-    A.cin = B.cell[0];
-    A.oxin = B.ox[0];
-    A.oyin = B.oy[0];
-    A.vxin = B.vx[0];
-    A.vyin = B.vy[0];
-    A.vzin = B.vz[0];
-    A.pidin = B.pid[0];
-    A.cout = B.cell[1];
-    A.oxout = B.ox[1];
-    A.oyout = B.oy[1];
-    A.vxout = B.vx[1];
-    A.vyout = B.vy[1];
-    A.vzout = B.vz[1];
-    A.pidout = B.pid[1];
+    const int to = 1 - from;
+    A.cin = B.cell[from];
+    A.oxin = B.ox[from];
+    A.oyin = B.oy[from];
+    A.vxin = B.vx[from];
+    A.vyin = B.vy[from];
+    A.vzin = B.vz[from];
+    A.pidin = B.pid[from];
+    A.cout = B.cell[to];
+    A.oxout = B.ox[to];
+    A.oyout = B.oy[to];
+    A.vxout = B.vx[to];
+    A.vyout = B.vy[to];
+    A.vzout = B.vz[to];
+    A.pidout = B.pid[to];
     const bool dsmc = h->dsmc.on && s == h->dsmc.s && h->dsmc.count;
     A.count = dsmc ? h->dsmc.count : h->count;
     A.cursor = h->cursor;
@@ -325,14 +326,15 @@ pic_status launch_recount(pic_handle *h, int s)
     return launch_hist(h, s, sort_args(h, s));
 }
 
-// Sort species s from buffer 0 into buffer 1 and compute the chunk anchors.
-// With counts_kept the DSMC species' pushes have kept its counts current since
-// they were last computed, and the histogram is skipped.
-pic_status launch_sort(pic_handle *h, int s, bool counts_kept)
+// Sort species s from buffer `from` into the other buffer (0 into 1 in the
+// step) and compute the chunk anchors.  With counts_kept the DSMC species'
+// pushes have kept its counts current since they were last computed, and
+// the histogram is skipped.
+pic_status launch_sort(pic_handle *h, int s, bool counts_kept, int from)
 {
     SpeciesBuf &B = h->sp[s];
     if (B.cap == 0) return PIC_OK;
-    const SortArgs A = sort_args(h, s);
+    const SortArgs A = sort_args(h, s, from);
     const bool dsmc = h->dsmc.on && s == h->dsmc.s && h->dsmc.count;
     const long long nkeys = A.nkeys;
     PIC_CUDA(cudaMemsetAsync(B.anchor, 0xFF, sizeof(int32_t) * (size_t)B.nchunks, h->stream));
