@@ -8,6 +8,8 @@
 // (particle id, block, 0, STREAM_INIT), so every particle's initial state
 // depends only on the seed and its id.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math.h>
 
 #include "pic_internal.cuh"
@@ -434,7 +436,7 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
 pic_status launch_from_global_records_range(pic_handle *h, int s, long long n, long long lo,
                                             long long hi, const double *x_dev, const double *y_dev,
                                             const double *vx_dev, const double *vy_dev,
-                                            const double *vz_dev)
+                                            const double *vz_dev, int max_blocks)
 {
     SpeciesBuf &B = h->sp[s];
     const long long cap = B.cap;
@@ -444,7 +446,9 @@ pic_status launch_from_global_records_range(pic_handle *h, int s, long long n, l
     const Geometry &g = h->g;
     const KeyGeo G = key_geo(g.nx, g.ny, g.tw, g.th, g.ntx, 0);
     uint32_t *scratch = (uint32_t *)h->stage;
-    from_global_records_kernel<<<grid_for(hi - lo, 256), 256, 0, h->stream>>>(
+    int grid = grid_for(hi - lo, 256);
+    if (max_blocks > 0) grid = std::min(grid, max_blocks);
+    from_global_records_kernel<<<grid, 256, 0, h->stream>>>(
         A, G, lo, hi, &h->dev->err, x_dev, y_dev, vx_dev, vy_dev, vz_dev, scratch,
         scratch + 2 * cap, reinterpret_cast<uint4 *>(scratch + 4 * cap));
     PIC_CUDA(cudaGetLastError());
@@ -456,7 +460,7 @@ pic_status launch_from_global_records(pic_handle *h, int s, long long n, const d
                                       const double *vy_dev, const double *vz_dev)
 {
     return launch_from_global_records_range(h, s, n, 0, h->sp[s].cap, x_dev, y_dev, vx_dev,
-                                            vy_dev, vz_dev);
+                                            vy_dev, vz_dev, 0);
 }
 
 // Export of species s in id order into five device arrays out[0..4] (x, y,

@@ -285,10 +285,12 @@ pic_status launch_from_global(pic_handle *h, int s, long long n, const double *x
                               const double *vz_dev);
 // the same conversion straight into the import sort's stage layout (keys,
 // slots and packed records of all cap slots; see import_sort)
+// (at most max_blocks blocks of 256 threads when max_blocks > 0, leaving the
+// rest of the GPU to kernels on other streams)
 pic_status launch_from_global_records_range(pic_handle *h, int s, long long n, long long lo,
                                             long long hi, const double *x_dev, const double *y_dev,
                                             const double *vx_dev, const double *vy_dev,
-                                            const double *vz_dev);
+                                            const double *vz_dev, int max_blocks);
 pic_status launch_from_global_records(pic_handle *h, int s, long long n, const double *x_dev,
                                       const double *y_dev, const double *vx_dev,
                                       const double *vy_dev, const double *vz_dev);
