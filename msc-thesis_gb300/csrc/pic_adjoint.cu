@@ -283,10 +283,14 @@ pic_status adjoint_run(pic_handle *h, const pic_init_spec *spec, long long nstep
     const float inv_eps0_n = (float)(1.0 / (c.eps0 * (double)ncell));
     // psi = S^T g and a_x += (q/dA) sum psi grad w at the positions in A
     auto solve_and_gather = [&]() -> pic_status {
-        PIC_CUFFT(cufftExecR2C(W.r2c2, gpl, (cufftComplex *)gh));
-        adj_kspace_kernel<<<gg, 256, 0, st>>>(gh, ph, g.nx, g.ny, g.nh, kx1, ky1, inv_eps0_n);
-        PIC_CUDA(cudaGetLastError());
-        PIC_CUFFT(cufftExecC2R(h->plan_c2r1, (cufftComplex *)ph, psi));
+        if (h->spectral) {
+            PIC_TRY(launch_spectral_adjoint(h, gpl, gpl + ncell, gh, ph, psi));
+        } else {
+            PIC_CUFFT(cufftExecR2C(W.r2c2, gpl, (cufftComplex *)gh));
+            adj_kspace_kernel<<<gg, 256, 0, st>>>(gh, ph, g.nx, g.ny, g.nh, kx1, ky1, inv_eps0_n);
+            PIC_CUDA(cudaGetLastError());
+            PIC_CUFFT(cufftExecC2R(h->plan_c2r1, (cufftComplex *)ph, psi));
+        }
         adj_gather_kernel<<<gp, 256, 0, st>>>(A);
         PIC_CUDA(cudaGetLastError());
         return PIC_OK;

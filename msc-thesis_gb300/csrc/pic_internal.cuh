@@ -250,6 +250,10 @@ bool spectral_size_ok(int nx, int ny);
 bool spectral_wanted(int nx, int ny);
 pic_status spectral_twiddles(int nx, int ny, float2 **tw);  // cudaMalloc'd tables
 pic_status launch_spectral(pic_handle *h);  // convert + solve, rho_fix cleared
+// the adjoint solve psi = S^T g (gx, gy -> psi) on a handle with h->spectral;
+// gh (2 ny nh) and ph (ny nh) are scratch
+pic_status launch_spectral_adjoint(pic_handle *h, const float *gx, const float *gy, float2 *gh,
+                                   float2 *ph, float *psi);
 struct EnsRun;
 // convert + solve of runs [first, first + count) of an ensemble's run table
 // (one grid size; grids at each run's offsets); rho_fix is not cleared

@@ -30,6 +30,7 @@
 #include <cmath>
 #include <vector>
 
+#include "pic_adjoint_dev.cuh"
 #include "pic_ensemble.cuh"
 #include "pic_fft_dev.cuh"
 #include "pic_field_dev.cuh"
@@ -48,7 +49,14 @@ struct SpecArgs {
     float scale;
     float kx1, ky1, inv_eps0_n;
     int tmx, tmy;
-    int pairs, cols, rows;  // row pairs, columns, rows per block of the three kernels
+    // adjoint solve (psi = S^T g): the two gradient planes in, their half
+    // spectra in S and Sy, psi^ after the inverse along y in Tx; the inverse
+    // rows take rows y ys and y ys + yo of Tx and Ty into ex and ey (ys = 1,
+    // yo = 0 for the field; 2 and 1 for psi, two rows per transform)
+    const float *gx, *gy;
+    float2 *Sy;
+    int ys, yo;
+    int pairs, cols, rows;  // transforms (row pairs or rows), columns, rows per block
     int sa, sb, sc;         // buffer strides (float2) of the three kernels
     DevState *dev;
     // ensemble: blockIdx.y picks run first + blockIdx.y of this table, whose
@@ -106,8 +114,9 @@ __device__ __forceinline__ T block_sum(T v, T *part)
     return s;
 }
 
-// LGX: log2 nx.  Block: `pairs` row pairs, nx/16 threads each.
-template <int LGX>
+// LGX: log2 nx.  Block: `pairs` transforms, nx/16 threads each: a pair of
+// density rows, or with ADJ one row of the two gradient planes (gx + i gy).
+template <int LGX, bool ADJ>
 __global__ void __launch_bounds__(256) spec_rows_fwd_kernel(SpecArgs P)
 {
     const SpecArgs A = block_args(P);
@@ -115,14 +124,18 @@ __global__ void __launch_bounds__(256) spec_rows_fwd_kernel(SpecArgs P)
     extern __shared__ float2 smem[];
     __shared__ unsigned long long s_q[32];
     const int f = threadIdx.x / TP, t = threadIdx.x - f * TP;
-    const int y0 = (blockIdx.x * A.pairs + f) * 2;
     float2 *buf[1] = {smem + f * A.sa};
     float2 v[1][fft::E];
     unsigned long long qs = 0;
-    {
+    if (ADJ) {
+        const size_t r0 = (size_t)(blockIdx.x * A.pairs + f) * NX;
+#pragma unroll
+        for (int k = 0; k < fft::E; ++k)
+            v[0][k] = make_float2(__ldg(A.gx + r0 + t + k * TP), __ldg(A.gy + r0 + t + k * TP));
+    } else {
         // all loads first (the density is read-only here), then the
         // conversions and the float density's stores
-        const size_t r0 = (size_t)y0 * NX;
+        const size_t r0 = (size_t)(blockIdx.x * A.pairs + f) * 2 * NX;
         unsigned long long a[fft::E], b[fft::E];
 #pragma unroll
         for (int k = 0; k < fft::E; ++k) {
@@ -144,25 +157,33 @@ __global__ void __launch_bounds__(256) spec_rows_fwd_kernel(SpecArgs P)
 #pragma unroll
     for (int k = 0; k < fft::E; ++k) buf[0][fft::pad(fft::result_index<LGX>(k, t))] = v[0][k];
     __syncthreads();
-    // split each pair's spectrum; (mode, pair) with the pair fastest, so that
-    // the block's rows of one mode are written together
+    // split each transform's spectrum; (mode, transform) with the transform
+    // fastest, so that the block's rows of one mode are written together
     const int np = A.pairs;
     for (int w = threadIdx.x; w < A.nh * np; w += blockDim.x) {
         const int ff = w % np, k = w / np;
         const float2 *bb = smem + ff * A.sa;
         const float2 z = bb[fft::pad(k)], m = bb[fft::pad((NX - k) & (NX - 1))];
-        const float4 ab = make_float4(0.5f * (z.x + m.x), 0.5f * (z.y - m.y), 0.5f * (z.y + m.y),
-                                      0.5f * (m.x - z.x));
-        const int yy = (blockIdx.x * np + ff) * 2;
-        *reinterpret_cast<float4 *>(A.S + (size_t)k * A.ny + yy) = ab;
+        const float2 ra = make_float2(0.5f * (z.x + m.x), 0.5f * (z.y - m.y));
+        const float2 rb = make_float2(0.5f * (z.y + m.y), 0.5f * (m.x - z.x));
+        if (ADJ) {
+            const size_t i = (size_t)k * A.ny + blockIdx.x * np + ff;
+            A.S[i] = ra;
+            A.Sy[i] = rb;
+        } else {
+            const int yy = (blockIdx.x * np + ff) * 2;
+            *reinterpret_cast<float4 *>(A.S + (size_t)k * A.ny + yy) = make_float4(ra.x, ra.y, rb.x, rb.y);
+        }
     }
-    qs = block_sum(qs, s_q);
-    if (threadIdx.x == 0) atomicAdd(&A.dev->q[acc_slot()], qs);
+    if (!ADJ) {
+        qs = block_sum(qs, s_q);
+        if (threadIdx.x == 0) atomicAdd(&A.dev->q[acc_slot()], qs);
+    }
 }
 
 // LGY: log2 ny.  Block: `cols` columns, ny/16 threads each; two buffers per
 // column (phi^, then Ey^).
-template <int LGY>
+template <int LGY, bool ADJ>
 __global__ void __launch_bounds__(256, 2) spec_cols_kernel(SpecArgs P)
 {
     const SpecArgs A = block_args(P);
@@ -176,16 +197,35 @@ __global__ void __launch_bounds__(256, 2) spec_cols_kernel(SpecArgs P)
     const size_t col = (size_t)(on ? mx : 0) * NY;
     float fe = 0.f;
     float2 v[1][fft::E];
-    {
-        float2 *buf[1] = {b0};
+    // forward transform of column `src` along y, left in natural order in `bs`
+    auto forward = [&](const float2 *src, float2 *bs) {
+        float2 *buf[1] = {bs};
 #pragma unroll
         for (int k = 0; k < fft::E; ++k)
-            v[0][k] = on ? __ldg(A.S + col + t + k * TP) : make_float2(0.f, 0.f);
+            v[0][k] = on ? __ldg(src + col + t + k * TP) : make_float2(0.f, 0.f);
         fft::transform<LGY, false, 1>(v, buf, t, A.twy);
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < fft::E; ++k) b0[fft::pad(fft::result_index<LGY>(k, t))] = v[0][k];
+        for (int k = 0; k < fft::E; ++k) bs[fft::pad(fft::result_index<LGY>(k, t))] = v[0][k];
         __syncthreads();
+    };
+    forward(A.S, b0);
+    if (ADJ) {
+        // psi^ = i (kx g^x + ky g^y) / (eps0 N k^2) per mode, inverse along y
+        forward(A.Sy, b1);
+#pragma unroll
+        for (int k = 0; k < fft::E; ++k) {
+            const int my = t + k * TP;
+            v[0][k] = adj_mode(b0[fft::pad(my)], b1[fft::pad(my)], mx, my, A.nx, NY, A.kx1, A.ky1,
+                               A.inv_eps0_n, mx == 0 && my == 0);
+        }
+        float2 *buf[1] = {b0};
+        fft::transform<LGY, true, 1>(v, buf, t, A.twy);
+        if (on) {
+#pragma unroll
+            for (int k = 0; k < fft::E; ++k) A.Tx[col + fft::result_index<LGY>(k, t)] = v[0][k];
+        }
+        return;
     }
     // k-space: phi^ stays in registers, Ey^ goes to the second buffer; the
     // two inverse transforms run one after the other
@@ -228,7 +268,8 @@ __global__ void __launch_bounds__(256, 2) spec_cols_kernel(SpecArgs P)
     if (threadIdx.x == 0) atomicAdd(&A.dev->fe[acc_slot()], sum);
 }
 
-// LGX: log2 nx.  Block: `rows` rows, nx/16 threads each.
+// LGX: log2 nx.  Block: `rows` transforms, nx/16 threads each: row y of Ex~
+// and Ey~ into Ex and Ey, or rows 2y and 2y + 1 of psi~ into psi.
 template <int LGX>
 __global__ void __launch_bounds__(256) spec_rows_inv_kernel(SpecArgs P)
 {
@@ -249,9 +290,9 @@ __global__ void __launch_bounds__(256) spec_rows_inv_kernel(SpecArgs P)
     for (int q = 0; q < ITEMS; ++q) {
         const int w = threadIdx.x + q * blockDim.x;
         if (w < total) {
-            const size_t i = (size_t)(w / nr) * A.ny + y0 + (w % nr);
+            const size_t i = (size_t)(w / nr) * A.ny + (size_t)(y0 + (w % nr)) * A.ys;
             X[q] = __ldg(A.Tx + i);
-            Y[q] = __ldg(A.Ty + i);
+            Y[q] = __ldg(A.Ty + i + A.yo);
         }
     }
 #pragma unroll
@@ -272,12 +313,12 @@ __global__ void __launch_bounds__(256) spec_rows_inv_kernel(SpecArgs P)
 #pragma unroll
     for (int k = 0; k < fft::E; ++k) v[0][k] = buf[0][fft::pad(t + k * TP)];
     fft::transform<LGX, true, 1>(v, buf, t, A.twx);
-    const size_t row = (size_t)(y0 + f) * NX;
+    const size_t rx = (size_t)(y0 + f) * A.ys * NX, ry = rx + (size_t)A.yo * NX;
 #pragma unroll
     for (int k = 0; k < fft::E; ++k) {
-        const size_t i = row + fft::result_index<LGX>(k, t);
-        A.ex[i] = v[0][k].x;
-        A.ey[i] = v[0][k].y;
+        const int i = fft::result_index<LGX>(k, t);
+        A.ex[rx + i] = v[0][k].x;
+        A.ey[ry + i] = v[0][k].y;
     }
 }
 
@@ -336,14 +377,20 @@ pic_status spectral_twiddles(int nx, int ny, float2 **tw)
 }
 
 // The three kernels over `batch` runs of one grid size (A.runs set) or one
-// run.  The caller clears the fixed-point density afterwards.
-static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st)
+// run: the field solve, or with adj the adjoint solve (A.gx, A.gy -> psi in
+// A.ex).  The caller clears the fixed-point density afterwards.
+static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st, bool adj = false)
 {
     const int nx = A.nx, ny = A.ny, nh = A.nh;
     A.lgx = ilog2(nx);
     A.lgy = ilog2(ny);
     A.twy = A.twx + fft::twiddle_len(A.lgx);
+    A.ys = adj ? 2 : 1;
+    A.yo = adj ? 1 : 0;
     const int tpx = nx >> 4, tpy = ny >> 4;
+    // transforms of the forward and the inverse rows: row pairs and rows
+    // (field), rows and row pairs (adjoint)
+    const int na = adj ? ny : ny / 2, nc = adj ? ny / 2 : ny;
     // transforms per block: at most 256 threads, and no more than spreads the
     // batch's transforms over about one block per SM (small grids otherwise
     // run on a few SMs), but at least a warp's worth where the grid allows
@@ -354,9 +401,9 @@ static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st)
         k = std::max(k, std::min(32 / tp, items));
         return std::max(1, std::min(k, items));
     };
-    A.pairs = per_block(tpx, ny / 2);
+    A.pairs = per_block(tpx, na);
     A.cols = per_block(tpy, nh);
-    A.rows = per_block(tpx, ny);
+    A.rows = per_block(tpx, nc);
     // interleaved buffers read by consecutive lanes start on different banks
     A.sa = fft::buf_stride(nx, 16 / std::min(A.pairs, 16));
     A.sb = fft::buf_stride(ny, 8);
@@ -368,7 +415,8 @@ static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st)
     switch (A.lgx) {
 #define PIC_SPEC_X(L)                                                                          \
     case L:                                                                                    \
-        ka = (const void *)spec_rows_fwd_kernel<L>;                                            \
+        ka = adj ? (const void *)spec_rows_fwd_kernel<L, true>                                 \
+                 : (const void *)spec_rows_fwd_kernel<L, false>;                               \
         kc = (const void *)spec_rows_inv_kernel<L>;                                            \
         break;
         PIC_SPEC_X(4) PIC_SPEC_X(5) PIC_SPEC_X(6) PIC_SPEC_X(7) PIC_SPEC_X(8) PIC_SPEC_X(9)
@@ -377,7 +425,9 @@ static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st)
     }
     switch (A.lgy) {
 #define PIC_SPEC_Y(L)                                                                          \
-    case L: kb = (const void *)spec_cols_kernel<L>; break;
+    case L:                                                                                    \
+        kb = adj ? (const void *)spec_cols_kernel<L, true> : (const void *)spec_cols_kernel<L, false>; \
+        break;
         PIC_SPEC_Y(4) PIC_SPEC_Y(5) PIC_SPEC_Y(6) PIC_SPEC_Y(7) PIC_SPEC_Y(8) PIC_SPEC_Y(9)
         PIC_SPEC_Y(10) PIC_SPEC_Y(11) PIC_SPEC_Y(12)
 #undef PIC_SPEC_Y
@@ -391,10 +441,10 @@ static pic_status launch_kernels(SpecArgs &A, int batch, cudaStream_t st)
     PIC_TRY(allow_dynamic_smem(kc, mc));
     void *args[] = {&A};
     const unsigned nb = (unsigned)batch;
-    PIC_CUDA(cudaLaunchKernel(ka, dim3(ny / (2 * A.pairs), nb), dim3(A.pairs * tpx), args, ma, st));
+    PIC_CUDA(cudaLaunchKernel(ka, dim3(na / A.pairs, nb), dim3(A.pairs * tpx), args, ma, st));
     PIC_CUDA(cudaLaunchKernel(kb, dim3((nh + A.cols - 1) / A.cols, nb), dim3(A.cols * tpy), args,
                               mb, st));
-    PIC_CUDA(cudaLaunchKernel(kc, dim3(ny / A.rows, nb), dim3(A.rows * tpx), args, mc, st));
+    PIC_CUDA(cudaLaunchKernel(kc, dim3(nc / A.rows, nb), dim3(A.rows * tpx), args, mc, st));
     return PIC_OK;
 }
 
@@ -449,6 +499,32 @@ pic_status launch_spectral_runs(const EnsRun *runs, int first, int count, int nx
     A.runs = runs;
     A.first = first;
     return launch_kernels(A, count, st);
+}
+
+// psi = S^T g on a power-of-two handle: gx, gy (ncell each) -> psi; gh
+// (2 ny nh) and ph (ny nh) are scratch
+pic_status launch_spectral_adjoint(pic_handle *h, const float *gx, const float *gy, float2 *gh,
+                                   float2 *ph, float *psi)
+{
+    const Geometry &g = h->g;
+    SpecArgs A;
+    memset(&A, 0, sizeof A);
+    A.gx = gx;
+    A.gy = gy;
+    A.S = gh;
+    A.Sy = gh + (size_t)g.nh * g.ny;
+    A.Tx = A.Ty = ph;
+    A.ex = A.ey = psi;
+    A.nx = g.nx;
+    A.ny = g.ny;
+    A.nh = g.nh;
+    A.twx = h->tw;
+    A.kx1 = (float)(2.0 * 3.14159265358979323846 / g.Lx);
+    A.ky1 = (float)(2.0 * 3.14159265358979323846 / g.Ly);
+    A.inv_eps0_n = (float)(1.0 / (h->cfg.eps0 * (double)g.nx * (double)g.ny));
+    A.tmx = A.tmy = -1;
+    A.dev = h->dev;
+    return launch_kernels(A, 1, h->stream, true);
 }
 
 }  // namespace pic
