@@ -90,3 +90,36 @@ def test_spectral_solve_matches_fp64_and_cufft(nx, ny):
     rel_e = np.abs(gs["ex_end"] - gc["ex_end"]).max() / np.abs(gc["ex_end"]).max()
     print(f"  after {NSTEPS} steps: FE {rel_fe:.2e}, mode (1,1) {rel_mode:.2e}, Ex {rel_e:.2e}")
     assert rel_fe < 1e-5 and rel_mode < 1e-5 and rel_e < 1e-4
+
+
+@pytest.mark.parametrize("nx,ny", [(64, 16), (32, 128)])
+def test_adjoint_solve_paths_agree(nx, ny):
+    """The adjoint's transposed solve (psi = S^T g) through the spectral
+    kernels' adjoint mode against cuFFT, on non-square grids: the final field
+    energy to 1e-5 and the gradients with respect to the initial state to
+    1e-3 over 20 steps (per-particle gradients carry each FP32 trajectory's
+    own cell crossings; a broken transposed solve errs by order one)."""
+    n = nx * ny * 16
+    Lx, Ly = 0.25 * nx, 0.25 * ny
+    cfg, _, _ = normalized_electrons(nx, ny, Lx, Ly, n, 0.1)
+    spec = P.init_spec(n, vth=(0.02, 0.02, 0.0), beam_v=0.2, pert_kind=P.PERT_XDISP,
+                       pert_amp=1e-3, pert_mx=1, seed=nx + ny)
+    out = {}
+    old = os.environ.get("PIC_FIELD_SOLVER")
+    try:
+        for solver in ("spectral", "cufft"):
+            os.environ["PIC_FIELD_SOLVER"] = solver
+            with P.Handle(cfg) as h:
+                h.init_particles(0, spec)
+                out[solver] = h.adjoint(20, every=10)
+    finally:
+        if old is None:
+            os.environ.pop("PIC_FIELD_SOLVER", None)
+        else:
+            os.environ["PIC_FIELD_SOLVER"] = old
+    rs, *gs = out["spectral"]
+    rc, *gc = out["cufft"]
+    errs = [np.linalg.norm(a - b) / np.linalg.norm(b) for a, b in zip(gs, gc)]
+    print(f"{nx}x{ny}: J {rs.J:.8e} vs {rc.J:.8e}; gradient rel norm differences", errs)
+    assert rs.J == pytest.approx(rc.J, rel=1e-5)
+    assert max(errs) < 1e-3
