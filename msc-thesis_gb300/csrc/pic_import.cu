@@ -208,12 +208,13 @@ pic_status import_sort(pic_handle *h, int s, bool *in_buffer0)
 // chunk would span eight tiles, so the caller then runs one counting sort
 // from buffer 1 into buffer 0: cheap on such data, whose every block of
 // particles spans a few cells of one range.
-// Conversion blocks of a range import: two 256-thread blocks per SM keep
+// Conversion blocks of a range import: four 256-thread blocks per SM keep
 // enough loads in flight for the link and leave the SMs' remaining threads
 // to the previous range's sort on the copy stream (2048^2 x 32 ppc, the
-// one-call run of 20 steps: 71.1 ms against 74.7, 75.9 and 72.8 ms with
-// 0.5, 1 and 8 blocks per SM, and 72.8 ms for the whole-array import)
-static int import_blocks() { return 2 * device_sms(); }
+// one-call run of 20 steps: 70.4 ms against 70.7, 71.0-71.8, 74.7 and
+// 72.8 ms with 3, 2, 0.5 and 8 blocks per SM, and 72.8 ms for the
+// whole-array import)
+static int import_blocks() { return 4 * device_sms(); }
 
 pic_status import_records_in_parts(pic_handle *h, int s, long long n, const double *x_dev,
                                    const double *y_dev, const double *vx_dev,

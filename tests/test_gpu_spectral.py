@@ -97,8 +97,8 @@ def test_adjoint_solve_paths_agree(nx, ny):
     """The adjoint's transposed solve (psi = S^T g) through the spectral
     kernels' adjoint mode against cuFFT, on non-square grids: the final field
     energy to 1e-5 and the gradients with respect to the initial state to
-    1e-3 over 20 steps (per-particle gradients carry each FP32 trajectory's
-    own cell crossings; a broken transposed solve errs by order one)."""
+    1e-4 over 20 steps (measured 2e-6 to 4e-6; per-particle gradients carry
+    each FP32 trajectory's own cell crossings)."""
     n = nx * ny * 16
     Lx, Ly = 0.25 * nx, 0.25 * ny
     cfg, _, _ = normalized_electrons(nx, ny, Lx, Ly, n, 0.1)
@@ -122,4 +122,4 @@ def test_adjoint_solve_paths_agree(nx, ny):
     errs = [np.linalg.norm(a - b) / np.linalg.norm(b) for a, b in zip(gs, gc)]
     print(f"{nx}x{ny}: J {rs.J:.8e} vs {rc.J:.8e}; gradient rel norm differences", errs)
     assert rs.J == pytest.approx(rc.J, rel=1e-5)
-    assert max(errs) < 1e-3
+    assert max(errs) < 1e-4
