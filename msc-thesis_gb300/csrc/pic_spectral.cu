@@ -18,6 +18,12 @@
 //             dropped, as a complex-to-real transform does), one inverse
 //             complex FFT, Ex = Re z, Ey = Im z.
 //
+// The same launches serve an ensemble's runs of one grid size (blockIdx.y
+// picks the run from the run table) and, in their adjoint mode, the
+// adjoint's transposed solve psi = S^T g (rows of gx + i gy forward, two
+// forward column transforms, the transposed k-space operator and one
+// inverse per column, two psi rows per inverse row transform).
+//
 // The arithmetic per mode is the k-space kernel's (pic_field_dev.cuh); the
 // transforms are pic_fft_dev.cuh's.  Replaces (reference paths inside
 // taylorj5/msc-thesis, thesisCode/collisionless/double/src/):
