@@ -169,6 +169,19 @@ def schedule(k, since_sort, S):
     return sorts, since_sort
 
 
+def timed_cadence(k, chosen):
+    """Sort cadence of a K-step timed region: the largest divisor of K not
+    above the chosen cadence, so that the K steps hold whole sort periods."""
+    return max(d for d in range(1, min(chosen, k) + 1) if k % d == 0)
+
+
+def warmup_alignment(warmup, S):
+    """Extra untimed steps after `warmup` (from a load, which sorts) so that
+    the warm-up ends on a sort-period boundary: the first timed step sorts."""
+    _, since = schedule(warmup, 0, S)
+    return S - since if since < S else 0
+
+
 def launches_for(k, since_sort, S, per_step, nspecies=1, per_sort=6):
     """Our kernels launched by k steps: per_step per step (single handle on a
     power-of-two grid: push, the three spectral-solve kernels, one
@@ -776,11 +789,10 @@ def main():
     # the timed steps hold whole sort periods: the cadence is the largest
     # divisor of K not above the chosen one, and the warm-up is extended to
     # end on a period boundary, so the K steps are K / S sorts and K steps
-    S = max(d for d in range(1, min(SORT_EVERY, args.steps) + 1) if args.steps % d == 0)
+    S = timed_cadence(args.steps, SORT_EVERY)
     cfg.sort_every = S
     SORT_EVERY = S
-    _, since = schedule(args.warmup, 0, S)
-    align = S - since if since < S else 0
+    align = warmup_alignment(args.warmup, S)
     h = P.Handle(cfg)
     h.init_particles(0, spec)
     h.prime_leapfrog()
