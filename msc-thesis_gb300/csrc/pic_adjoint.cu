@@ -213,14 +213,14 @@ pic_status adjoint_run(pic_handle *h, const pic_init_spec *spec, long long nstep
     Snap fin;
     PIC_TRY(snap_alloc(W, fin, np));
     // ring of one segment: positions and fields per step
-    int32_t *rc;
-    float *rox, *roy, *re;
+    int32_t *rc = nullptr;
+    float *rox = nullptr, *roy = nullptr, *re = nullptr;
     PIC_TRY(W.alloc(&rc, np * K));
     PIC_TRY(W.alloc(&rox, np * K));
     PIC_TRY(W.alloc(&roy, np * K));
     PIC_TRY(W.alloc(&re, 2 * ncell * K));
-    float *ax, *ay, *avx, *avy, *gpl, *psi;
-    float2 *gh, *ph;
+    float *ax = nullptr, *ay = nullptr, *avx = nullptr, *avy = nullptr, *gpl = nullptr, *psi = nullptr;
+    float2 *gh = nullptr, *ph = nullptr;
     PIC_TRY(W.alloc(&ax, np));
     PIC_TRY(W.alloc(&ay, np));
     PIC_TRY(W.alloc(&avx, np));

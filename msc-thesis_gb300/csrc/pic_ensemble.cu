@@ -814,16 +814,16 @@ pic_status pic_ensemble_init(pic_ensemble *e, const pic_init_spec *specs)
         PIC_CUDA(cudaMemGetInfo(&free_b, &total_b));
         const bool packed = free_b >= 48 * ns + (1ull << 30);
         PIC_CUDA(cudaMalloc(&scratch, (packed ? 48 : 16) * ns));
-        pic_status s_ = ens_import_sort(e, scratch, packed, &temp, &temp_bytes);
-        if (s_ == PIC_OK && e->npush) {
+        pic_status sorted = ens_import_sort(e, scratch, packed, &temp, &temp_bytes);
+        if (sorted == PIC_OK && e->npush) {
             ens_anchor_kernel<<<(e->npush + 255) / 256, 256, 0, st>>>(e->cell[1], e->push_blk,
                                                                       e->d_runs, e->npush, e->anchor);
-            if (cudaGetLastError() != cudaSuccess) s_ = PIC_ERR_CUDA;
+            if (cudaGetLastError() != cudaSuccess) sorted = PIC_ERR_CUDA;
         }
         cudaStreamSynchronize(st);
         cudaFree(scratch);
         if (temp) cudaFree(temp);
-        PIC_TRY(s_);
+        PIC_TRY(sorted);
     }
     PIC_TRY(ens_launch_push(e, 1, 2));
     PIC_TRY(ens_poisson(e));
