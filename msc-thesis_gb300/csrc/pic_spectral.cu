@@ -503,8 +503,12 @@ pic_status launch_spectral_runs(const EnsRun *runs, int first, int count, int nx
     A.tmx = A.tmy = -1;
     A.dev = devs;
     A.runs = runs;
-    A.first = first;
-    return launch_kernels(A, count, st);
+    // a grid's y dimension holds at most 65535 runs
+    for (int b = 0; b < count; b += 65535) {
+        A.first = first + b;
+        PIC_TRY(launch_kernels(A, std::min(65535, count - b), st));
+    }
+    return PIC_OK;
 }
 
 // psi = S^T g on a power-of-two handle: gx, gy (ncell each) -> psi; gh
